@@ -1,0 +1,549 @@
+// gmle_runtime.cu - the C ABI of libgaussmle_sm100a.so (include/gaussmle_gb300.h).
+//
+// Host runtime around the fit kernels: device context, resident calibration
+// maps, launch-shape selection, and the host-buffer fit pipeline that replaces
+// the per-batch allocate / copyto! / launch / synchronize / copy-back loop of
+// GaussMLE.fit (src/interface.jl:220-262, :336-369, :423-456).  Each context
+// owns three CUDA streams (H2D copies, kernels, D2H copies) and two pipeline
+// slots, so that chunk k+1 is copied in while chunk k is fitted and chunk k-1
+// is copied out.  Device and pinned buffers grow on demand and are reused by
+// later calls; nothing the library allocates is handed to the caller.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+
+#include "../../include/gaussmle_gb300.h"
+#include "gmle_launch.cuh"
+
+namespace {
+
+using gmle::KernelArgs;
+
+int nparams(int model) { return model == 0 ? 4 : (model == 2 ? 6 : 5); }
+
+struct Tuning {
+    int tpr;
+    int rois_per_block;
+};
+
+// One pipeline slot of device buffers for the host-buffer path.
+struct Slot {
+    float *data = nullptr;
+    int32_t *xc = nullptr, *yc = nullptr;
+    float *params = nullptr, *crlb = nullptr, *llr = nullptr;
+    uint8_t *flags = nullptr;
+    int64_t cap_rois = 0;   // ROIs the buffers hold
+    int64_t cap_b2 = 0;     // box^2 the data buffer was sized for
+    // pinned staging for pageable caller memory
+    float *h_data = nullptr;
+    float *h_params = nullptr, *h_crlb = nullptr, *h_llr = nullptr;
+    uint8_t *h_flags = nullptr;
+    int64_t h_cap_rois = 0, h_cap_b2 = 0;
+    cudaEvent_t h2d_done = nullptr, fit_done = nullptr, d2h_done = nullptr;
+    // pending copy of pinned outputs to pageable caller memory
+    bool pending = false;
+    float *dst_params = nullptr, *dst_crlb = nullptr, *dst_llr = nullptr;
+    uint8_t *dst_flags = nullptr;
+    int64_t pend_rois = 0;
+    int pend_p = 0;
+};
+
+}  // namespace
+
+struct gmle_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t s_fit = nullptr, s_h2d = nullptr, s_d2h = nullptr;
+    std::string err;
+    std::mutex mu;
+    // resident calibration maps, (ny, nx) column-major
+    float *d_var = nullptr, *d_gain = nullptr, *d_offset = nullptr;
+    int32_t ny = 0, nx = 0;
+    unsigned long long *d_bad = nullptr;
+    int64_t launches = 0;
+    std::map<std::tuple<int, int, int>, Tuning> tuning;
+    Slot slots[2];
+};
+
+namespace {
+
+gmle_status fail(gmle_ctx *ctx, gmle_status st, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (ctx) ctx->err = buf;
+    return st;
+}
+
+gmle_status cuda_fail(gmle_ctx *ctx, cudaError_t e, const char *what)
+{
+    if (e == cudaErrorMemoryAllocation)
+        return fail(ctx, GMLE_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+    return fail(ctx, GMLE_CUDA_ERROR, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call, what)                                      \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
+    } while (0)
+
+gmle_status check_desc(gmle_ctx *ctx, const gmle_fit_desc *d)
+{
+    if (!d) return fail(ctx, GMLE_INVALID_ARG, "desc is NULL");
+    if (d->model < 0 || d->model > 3)
+        return fail(ctx, GMLE_UNSUPPORTED_MODEL, "unknown model id %d", d->model);
+    if (!gmle::box_supported(d->box))
+        return fail(ctx, GMLE_UNSUPPORTED_BOX, "box size %d has no compiled kernel (5..15 odd)",
+                    d->box);
+    if (d->iterations < 0) return fail(ctx, GMLE_INVALID_ARG, "iterations < 0");
+    if (d->camera < 0 || d->camera > 2)
+        return fail(ctx, GMLE_INVALID_ARG, "unknown camera id %d", d->camera);
+    if (d->camera != GMLE_CAMERA_POISSON) {
+        if (!ctx->d_var) return fail(ctx, GMLE_INVALID_ARG, "sCMOS fit without calibration maps");
+        if (d->camera == GMLE_CAMERA_SCMOS_ADU && (!ctx->d_gain || !ctx->d_offset))
+            return fail(ctx, GMLE_INVALID_ARG, "ADU fit needs gain and offset maps");
+    }
+    if (d->model == GMLE_MODEL_XYNB && !(d->psf[0] > 0.f))
+        return fail(ctx, GMLE_INVALID_ARG, "GaussianXYNB sigma must be > 0");
+    if (d->model == GMLE_MODEL_ASTIG && (!(d->psf[0] > 0.f) || !(d->psf[1] > 0.f) || d->psf[7] == 0.f))
+        return fail(ctx, GMLE_INVALID_ARG, "astigmatic sigma0 must be > 0 and d != 0");
+    return GMLE_OK;
+}
+
+// Launch shape: enough threads to fill the GPU (threads per ROI grows for small
+// batches), and ROIs per block bounded by shared memory.
+Tuning default_tuning(const gmle_ctx *ctx, int model, int box, bool scmos, int64_t n)
+{
+    const int64_t target_threads = (int64_t)ctx->num_sms * 1024;
+    int tpr = 1;
+    while (tpr < 8 && n * tpr < target_threads) tpr *= 2;
+    int threads = 128;
+    int rpb = threads / tpr;
+    while (rpb > 1 && gmle::smem_bytes(model, box, scmos, tpr, rpb) > 72 * 1024) {
+        threads /= 2;
+        rpb = threads / tpr;
+    }
+    if (rpb * tpr < 32) rpb = 32 / tpr;
+    return {tpr, rpb};
+}
+
+Tuning pick_tuning(gmle_ctx *ctx, const gmle_fit_desc *d, int64_t n)
+{
+    const bool scmos = d->camera != GMLE_CAMERA_POISSON;
+    auto it = ctx->tuning.find({d->model, d->box, (int)scmos});
+    if (it != ctx->tuning.end()) return it->second;
+    return default_tuning(ctx, d->model, d->box, scmos, n);
+}
+
+KernelArgs make_args(gmle_ctx *ctx, const gmle_fit_desc *d, const float *data, const int32_t *xc,
+                     const int32_t *yc, int64_t n, float *params, float *crlb, float *llr,
+                     uint8_t *flags, int tpr)
+{
+    KernelArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.data = data;
+    a.xc = xc;
+    a.yc = yc;
+    a.n = n;
+    a.var = ctx->d_var;
+    a.gain = ctx->d_gain;
+    a.offset = ctx->d_offset;
+    a.ny = ctx->ny;
+    a.nx = ctx->nx;
+    a.adu = d->camera == GMLE_CAMERA_SCMOS_ADU;
+    a.iterations = d->iterations;
+    a.tpr = tpr;
+    // sqrt(two * one(T) * pi) in Float32, as src/gausslib/baselibrary.jl:26 evaluates it
+    a.sqrt2pi = sqrtf(2.0f * (float)3.14159265358979323846);
+    std::memcpy(a.psf, d->psf, sizeof a.psf);
+    std::memcpy(a.lower, d->lower, sizeof a.lower);
+    std::memcpy(a.upper, d->upper, sizeof a.upper);
+    std::memcpy(a.max_step, d->max_step, sizeof a.max_step);
+    a.params = params;
+    a.crlb = crlb;
+    a.llr = llr;
+    a.flags = flags;
+    a.bad_corners = ctx->d_bad;
+    return a;
+}
+
+cudaError_t launch(gmle_ctx *ctx, const gmle_fit_desc *d, const KernelArgs &a, int rpb,
+                   cudaStream_t s)
+{
+    const bool scmos = d->camera != GMLE_CAMERA_POISSON;
+    ctx->launches++;
+    switch (d->model) {
+        case 0: return gmle::launch_fit_model0(d->box, scmos, a, rpb, s);
+        case 1: return gmle::launch_fit_model1(d->box, scmos, a, rpb, s);
+        case 2: return gmle::launch_fit_model2(d->box, scmos, a, rpb, s);
+        default: return gmle::launch_fit_model3(d->box, scmos, a, rpb, s);
+    }
+}
+
+bool is_pinned(const void *p)
+{
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return attr.type == cudaMemoryTypeHost;
+}
+
+void free_slot(Slot &s)
+{
+    cudaFree(s.data);
+    cudaFree(s.xc);
+    cudaFree(s.yc);
+    cudaFree(s.params);
+    cudaFree(s.crlb);
+    cudaFree(s.llr);
+    cudaFree(s.flags);
+    cudaFreeHost(s.h_data);
+    cudaFreeHost(s.h_params);
+    cudaFreeHost(s.h_crlb);
+    cudaFreeHost(s.h_llr);
+    cudaFreeHost(s.h_flags);
+    if (s.h2d_done) cudaEventDestroy(s.h2d_done);
+    if (s.fit_done) cudaEventDestroy(s.fit_done);
+    if (s.d2h_done) cudaEventDestroy(s.d2h_done);
+    s = Slot();
+}
+
+gmle_status ensure_slot(gmle_ctx *ctx, Slot &s, int64_t rois, int64_t b2, bool need_pinned)
+{
+    if (!s.h2d_done) {
+        CK(cudaEventCreateWithFlags(&s.h2d_done, cudaEventDisableTiming), "cudaEventCreate");
+        CK(cudaEventCreateWithFlags(&s.fit_done, cudaEventDisableTiming), "cudaEventCreate");
+        CK(cudaEventCreateWithFlags(&s.d2h_done, cudaEventDisableTiming), "cudaEventCreate");
+    }
+    if (s.cap_rois < rois || s.cap_b2 < b2) {
+        cudaFree(s.data); cudaFree(s.xc); cudaFree(s.yc);
+        cudaFree(s.params); cudaFree(s.crlb); cudaFree(s.llr); cudaFree(s.flags);
+        s.data = nullptr; s.xc = s.yc = nullptr; s.params = s.crlb = s.llr = nullptr; s.flags = nullptr;
+        s.cap_rois = s.cap_b2 = 0;
+        CK(cudaMalloc(&s.data, sizeof(float) * rois * b2), "cudaMalloc(data)");
+        CK(cudaMalloc(&s.xc, sizeof(int32_t) * rois), "cudaMalloc(corners)");
+        CK(cudaMalloc(&s.yc, sizeof(int32_t) * rois), "cudaMalloc(corners)");
+        CK(cudaMalloc(&s.params, sizeof(float) * rois * 6), "cudaMalloc(params)");
+        CK(cudaMalloc(&s.crlb, sizeof(float) * rois * 6), "cudaMalloc(crlb)");
+        CK(cudaMalloc(&s.llr, sizeof(float) * rois), "cudaMalloc(llr)");
+        CK(cudaMalloc(&s.flags, rois), "cudaMalloc(flags)");
+        s.cap_rois = rois;
+        s.cap_b2 = b2;
+    }
+    if (need_pinned && (s.h_cap_rois < rois || s.h_cap_b2 < b2)) {
+        cudaFreeHost(s.h_data); cudaFreeHost(s.h_params); cudaFreeHost(s.h_crlb);
+        cudaFreeHost(s.h_llr); cudaFreeHost(s.h_flags);
+        s.h_data = nullptr; s.h_params = s.h_crlb = s.h_llr = nullptr; s.h_flags = nullptr;
+        s.h_cap_rois = s.h_cap_b2 = 0;
+        CK(cudaMallocHost(&s.h_data, sizeof(float) * rois * b2), "cudaMallocHost(data)");
+        CK(cudaMallocHost(&s.h_params, sizeof(float) * rois * 6), "cudaMallocHost(params)");
+        CK(cudaMallocHost(&s.h_crlb, sizeof(float) * rois * 6), "cudaMallocHost(crlb)");
+        CK(cudaMallocHost(&s.h_llr, sizeof(float) * rois), "cudaMallocHost(llr)");
+        CK(cudaMallocHost(&s.h_flags, rois), "cudaMallocHost(flags)");
+        s.h_cap_rois = rois;
+        s.h_cap_b2 = b2;
+    }
+    return GMLE_OK;
+}
+
+// Copy a finished slot's pinned outputs to the caller's pageable buffers.
+gmle_status flush_slot(gmle_ctx *ctx, Slot &s)
+{
+    if (!s.pending) return GMLE_OK;
+    CK(cudaEventSynchronize(s.d2h_done), "cudaEventSynchronize");
+    std::memcpy(s.dst_params, s.h_params, sizeof(float) * s.pend_rois * s.pend_p);
+    std::memcpy(s.dst_crlb, s.h_crlb, sizeof(float) * s.pend_rois * s.pend_p);
+    std::memcpy(s.dst_llr, s.h_llr, sizeof(float) * s.pend_rois);
+    if (s.dst_flags) std::memcpy(s.dst_flags, s.h_flags, s.pend_rois);
+    s.pending = false;
+    return GMLE_OK;
+}
+
+gmle_status check_corners_host(gmle_ctx *ctx, const gmle_fit_desc *d, const int32_t *xc,
+                               const int32_t *yc, int64_t n)
+{
+    if (d->camera == GMLE_CAMERA_POISSON) return GMLE_OK;
+    if (!xc || !yc) return fail(ctx, GMLE_INVALID_ARG, "sCMOS fit needs ROI corners");
+    for (int64_t k = 0; k < n; k++) {
+        const int64_t x = xc[k], y = yc[k];
+        if (x < 1 || y < 1 || x + d->box - 1 > ctx->nx || y + d->box - 1 > ctx->ny)
+            return fail(ctx, GMLE_INVALID_ARG,
+                        "ROI %lld: corner (x=%lld, y=%lld) puts the %dx%d box outside the %dx%d "
+                        "calibration map",
+                        (long long)k, (long long)x, (long long)y, d->box, d->box, ctx->ny, ctx->nx);
+    }
+    return GMLE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gmle_abi_version(void) { return GMLE_ABI_VERSION; }
+
+gmle_status gmle_create(gmle_ctx **out, int device_ordinal)
+{
+    if (!out) return GMLE_INVALID_ARG;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return GMLE_NO_DEVICE;
+    }
+    if (device_ordinal < 0 || device_ordinal >= count) return GMLE_NO_DEVICE;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device_ordinal) != cudaSuccess) return GMLE_NO_DEVICE;
+    // The kernels are built for sm_103a only.
+    if (prop.major != 10 || prop.minor != 3) return GMLE_NO_DEVICE;
+    gmle_ctx *ctx = new gmle_ctx();
+    ctx->device = device_ordinal;
+    ctx->num_sms = prop.multiProcessorCount;
+    cudaSetDevice(device_ordinal);
+    if (cudaStreamCreateWithFlags(&ctx->s_fit, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->s_h2d, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->s_d2h, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&ctx->d_bad, sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMemset(ctx->d_bad, 0, sizeof(unsigned long long)) != cudaSuccess) {
+        cudaGetLastError();
+        gmle_destroy(ctx);
+        return GMLE_CUDA_ERROR;
+    }
+    *out = ctx;
+    return GMLE_OK;
+}
+
+void gmle_destroy(gmle_ctx *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->s_fit) cudaStreamSynchronize(ctx->s_fit);
+    if (ctx->s_h2d) cudaStreamSynchronize(ctx->s_h2d);
+    if (ctx->s_d2h) cudaStreamSynchronize(ctx->s_d2h);
+    for (Slot &s : ctx->slots) free_slot(s);
+    cudaFree(ctx->d_var);
+    cudaFree(ctx->d_gain);
+    cudaFree(ctx->d_offset);
+    cudaFree(ctx->d_bad);
+    if (ctx->s_fit) cudaStreamDestroy(ctx->s_fit);
+    if (ctx->s_h2d) cudaStreamDestroy(ctx->s_h2d);
+    if (ctx->s_d2h) cudaStreamDestroy(ctx->s_d2h);
+    delete ctx;
+}
+
+const char *gmle_last_error(const gmle_ctx *ctx)
+{
+    if (!ctx) return "no context";
+    return ctx->err.c_str();
+}
+
+gmle_status gmle_set_calibration(gmle_ctx *ctx, const float *variance, const float *gain,
+                                 const float *offset, int32_t ny, int32_t nx)
+{
+    if (!ctx) return GMLE_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (!variance || ny <= 0 || nx <= 0)
+        return fail(ctx, GMLE_INVALID_ARG, "variance map and positive ny, nx are required");
+    if ((gain == nullptr) != (offset == nullptr))
+        return fail(ctx, GMLE_INVALID_ARG, "gain and offset maps come together");
+    cudaSetDevice(ctx->device);
+    CK(cudaStreamSynchronize(ctx->s_fit), "cudaStreamSynchronize");
+    cudaFree(ctx->d_var);
+    cudaFree(ctx->d_gain);
+    cudaFree(ctx->d_offset);
+    ctx->d_var = ctx->d_gain = ctx->d_offset = nullptr;
+    ctx->ny = ctx->nx = 0;
+    const size_t bytes = sizeof(float) * (size_t)ny * (size_t)nx;
+    CK(cudaMalloc(&ctx->d_var, bytes), "cudaMalloc(variance)");
+    CK(cudaMemcpy(ctx->d_var, variance, bytes, cudaMemcpyHostToDevice), "upload variance");
+    if (gain) {
+        CK(cudaMalloc(&ctx->d_gain, bytes), "cudaMalloc(gain)");
+        CK(cudaMalloc(&ctx->d_offset, bytes), "cudaMalloc(offset)");
+        CK(cudaMemcpy(ctx->d_gain, gain, bytes, cudaMemcpyHostToDevice), "upload gain");
+        CK(cudaMemcpy(ctx->d_offset, offset, bytes, cudaMemcpyHostToDevice), "upload offset");
+    }
+    ctx->ny = ny;
+    ctx->nx = nx;
+    return GMLE_OK;
+}
+
+gmle_status gmle_fit_device(gmle_ctx *ctx, const gmle_fit_desc *desc, const float *d_data,
+                            const int32_t *d_x_corners, const int32_t *d_y_corners, int64_t n,
+                            float *d_params, float *d_crlb, float *d_llr, uint8_t *d_flags,
+                            void *stream)
+{
+    if (!ctx) return GMLE_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    gmle_status st = check_desc(ctx, desc);
+    if (st != GMLE_OK) return st;
+    if (n < 0) return fail(ctx, GMLE_INVALID_ARG, "n < 0");
+    if (n == 0) return GMLE_OK;
+    if (!d_data || !d_params || !d_crlb || !d_llr)
+        return fail(ctx, GMLE_INVALID_ARG, "data and output pointers are required");
+    if (desc->camera != GMLE_CAMERA_POISSON && (!d_x_corners || !d_y_corners))
+        return fail(ctx, GMLE_INVALID_ARG, "sCMOS fit needs ROI corners");
+    cudaSetDevice(ctx->device);
+    const Tuning t = pick_tuning(ctx, desc, n);
+    KernelArgs a = make_args(ctx, desc, d_data, d_x_corners, d_y_corners, n, d_params, d_crlb,
+                             d_llr, d_flags, t.tpr);
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->s_fit;
+    CK(launch(ctx, desc, a, t.rois_per_block, s), "fit kernel launch");
+    return GMLE_OK;
+}
+
+gmle_status gmle_fit_device_errors(gmle_ctx *ctx, int64_t *count)
+{
+    if (!ctx || !count) return GMLE_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    unsigned long long v = 0;
+    CK(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+    CK(cudaMemcpy(&v, ctx->d_bad, sizeof v, cudaMemcpyDeviceToHost), "read error counter");
+    CK(cudaMemset(ctx->d_bad, 0, sizeof v), "reset error counter");
+    *count = (int64_t)v;
+    return GMLE_OK;
+}
+
+gmle_status gmle_fit(gmle_ctx *ctx, const gmle_fit_desc *desc, const float *data,
+                     const int32_t *x_corners, const int32_t *y_corners, int64_t n,
+                     float *params, float *crlb, float *llr, uint8_t *flags)
+{
+    if (!ctx) return GMLE_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    gmle_status st = check_desc(ctx, desc);
+    if (st != GMLE_OK) return st;
+    if (n < 0) return fail(ctx, GMLE_INVALID_ARG, "n < 0");
+    if (n == 0) return GMLE_OK;
+    if (!data || !params || !crlb || !llr)
+        return fail(ctx, GMLE_INVALID_ARG, "data and output pointers are required");
+    st = check_corners_host(ctx, desc, x_corners, y_corners, n);
+    if (st != GMLE_OK) return st;
+    cudaSetDevice(ctx->device);
+
+    const int P = nparams(desc->model);
+    const int64_t b2 = (int64_t)desc->box * desc->box;
+    const bool scmos = desc->camera != GMLE_CAMERA_POISSON;
+    // Chunk of about 64 MiB of pixel data, at least one full GPU wave.
+    int64_t chunk = std::max<int64_t>((int64_t)ctx->num_sms * 1024, (64ll << 20) / (4 * b2));
+    chunk = std::min<int64_t>(chunk, n);
+    const bool in_pinned = is_pinned(data);
+    const bool out_pinned = is_pinned(params) && is_pinned(crlb) && is_pinned(llr) &&
+                            (!flags || is_pinned(flags));
+    const Tuning t = pick_tuning(ctx, desc, chunk);
+
+    for (Slot &s : ctx->slots) {
+        st = ensure_slot(ctx, s, chunk, b2, !(in_pinned && out_pinned));
+        if (st != GMLE_OK) return st;
+    }
+    int k = 0;
+    for (int64_t off = 0; off < n; off += chunk, k ^= 1) {
+        Slot &s = ctx->slots[k];
+        const int64_t m = std::min(chunk, n - off);
+        // The slot's previous chunk must be out before its buffers are reused.
+        st = flush_slot(ctx, s);
+        if (st != GMLE_OK) return st;
+        CK(cudaStreamWaitEvent(ctx->s_h2d, s.d2h_done, 0), "cudaStreamWaitEvent");
+        const float *src = data + off * b2;
+        if (!in_pinned) {
+            CK(cudaEventSynchronize(s.h2d_done), "cudaEventSynchronize");
+            std::memcpy(s.h_data, src, sizeof(float) * m * b2);
+            src = s.h_data;
+        }
+        CK(cudaMemcpyAsync(s.data, src, sizeof(float) * m * b2, cudaMemcpyHostToDevice, ctx->s_h2d),
+           "H2D data");
+        if (scmos) {
+            CK(cudaMemcpyAsync(s.xc, x_corners + off, sizeof(int32_t) * m, cudaMemcpyHostToDevice,
+                               ctx->s_h2d), "H2D corners");
+            CK(cudaMemcpyAsync(s.yc, y_corners + off, sizeof(int32_t) * m, cudaMemcpyHostToDevice,
+                               ctx->s_h2d), "H2D corners");
+        }
+        CK(cudaEventRecord(s.h2d_done, ctx->s_h2d), "cudaEventRecord");
+        CK(cudaStreamWaitEvent(ctx->s_fit, s.h2d_done, 0), "cudaStreamWaitEvent");
+        KernelArgs a = make_args(ctx, desc, s.data, scmos ? s.xc : nullptr, scmos ? s.yc : nullptr,
+                                 m, s.params, s.crlb, s.llr, s.flags, t.tpr);
+        CK(launch(ctx, desc, a, t.rois_per_block, ctx->s_fit), "fit kernel launch");
+        CK(cudaEventRecord(s.fit_done, ctx->s_fit), "cudaEventRecord");
+        CK(cudaStreamWaitEvent(ctx->s_d2h, s.fit_done, 0), "cudaStreamWaitEvent");
+        float *op = out_pinned ? params + off * P : s.h_params;
+        float *oc = out_pinned ? crlb + off * P : s.h_crlb;
+        float *ol = out_pinned ? llr + off : s.h_llr;
+        uint8_t *of = out_pinned ? (flags ? flags + off : nullptr) : s.h_flags;
+        CK(cudaMemcpyAsync(op, s.params, sizeof(float) * m * P, cudaMemcpyDeviceToHost, ctx->s_d2h),
+           "D2H params");
+        CK(cudaMemcpyAsync(oc, s.crlb, sizeof(float) * m * P, cudaMemcpyDeviceToHost, ctx->s_d2h),
+           "D2H crlb");
+        CK(cudaMemcpyAsync(ol, s.llr, sizeof(float) * m, cudaMemcpyDeviceToHost, ctx->s_d2h),
+           "D2H llr");
+        if (of)
+            CK(cudaMemcpyAsync(of, s.flags, m, cudaMemcpyDeviceToHost, ctx->s_d2h), "D2H flags");
+        CK(cudaEventRecord(s.d2h_done, ctx->s_d2h), "cudaEventRecord");
+        if (!out_pinned) {
+            s.pending = true;
+            s.dst_params = params + off * P;
+            s.dst_crlb = crlb + off * P;
+            s.dst_llr = llr + off;
+            s.dst_flags = flags ? flags + off : nullptr;
+            s.pend_rois = m;
+            s.pend_p = P;
+        }
+    }
+    for (Slot &s : ctx->slots) {
+        st = flush_slot(ctx, s);
+        if (st != GMLE_OK) return st;
+    }
+    CK(cudaStreamSynchronize(ctx->s_d2h), "cudaStreamSynchronize");
+    CK(cudaStreamSynchronize(ctx->s_fit), "cudaStreamSynchronize");
+    return GMLE_OK;
+}
+
+gmle_status gmle_get_tuning(gmle_ctx *ctx, int32_t model, int32_t box, int32_t camera,
+                            int32_t *threads_per_roi, int32_t *rois_per_block)
+{
+    if (!ctx || !threads_per_roi || !rois_per_block) return GMLE_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    const bool scmos = camera != GMLE_CAMERA_POISSON;
+    auto it = ctx->tuning.find({model, box, (int)scmos});
+    Tuning t = it != ctx->tuning.end() ? it->second
+                                       : default_tuning(ctx, model, box, scmos, 1ll << 40);
+    *threads_per_roi = t.tpr;
+    *rois_per_block = t.rois_per_block;
+    return GMLE_OK;
+}
+
+gmle_status gmle_set_tuning(gmle_ctx *ctx, int32_t model, int32_t box, int32_t camera,
+                            int32_t threads_per_roi, int32_t rois_per_block)
+{
+    if (!ctx) return GMLE_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    const int tpr = threads_per_roi;
+    if (tpr < 1 || tpr > 32 || (tpr & (tpr - 1)))
+        return fail(ctx, GMLE_INVALID_ARG, "threads_per_roi must be a power of two in 1..32");
+    if (model < 0 || model > 3) return fail(ctx, GMLE_UNSUPPORTED_MODEL, "unknown model");
+    if (!gmle::box_supported(box)) return fail(ctx, GMLE_UNSUPPORTED_BOX, "unsupported box");
+    const bool scmos = camera != GMLE_CAMERA_POISSON;
+    const int threads = tpr * rois_per_block;
+    if (rois_per_block < 1 || threads > 256 || threads % 32)
+        return fail(ctx, GMLE_INVALID_ARG,
+                    "threads_per_roi * rois_per_block must be a multiple of 32, at most 256");
+    if (gmle::smem_bytes(model, box, scmos, tpr, rois_per_block) > 227 * 1024)
+        return fail(ctx, GMLE_INVALID_ARG, "launch shape needs more than 227 KiB shared memory");
+    ctx->tuning[{model, box, (int)scmos}] = {tpr, rois_per_block};
+    return GMLE_OK;
+}
+
+int64_t gmle_kernel_launches(const gmle_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,167 @@
+/*
+ * gaussmle_gb300.h - C ABI of libgaussmle_sm100a.so, the GB300 (sm_103a)
+ * implementation of GaussMLE.jl's batched per-ROI Gaussian MLE fit.
+ *
+ * The library replaces the GPU branches of GaussMLE.fit
+ * (src/interface.jl:217-263 for fit(Array), :334-370 for fit(ROIBatch{IdealCamera}),
+ * :421-457 for fit(ROIBatch{SCMOSCamera})): every per-batch KernelAbstractions
+ * allocate/copyto!/launch/synchronize/copy-back cycle becomes one call here.
+ * Everything before those branches (input validation, to_pixel_units, corner
+ * vectors) and after them (p-values, create_localization_result, to_smld)
+ * stays on the caller's side, so the caller still builds the same emitters.
+ *
+ * Conventions (the reference's, src/unified_kernel.jl:285-297):
+ *  - data is Float32 (box, box, n) column-major: pixel (i = row = y,
+ *    j = column = x) of ROI k is data[(i-1) + box*(j-1) + box*box*k];
+ *  - camera maps are Float32 (ny, nx) column-major, map[row = y, col = x];
+ *  - corners are 1-based Int32 (Julia): ROI pixel (i, j) of ROI k lies on
+ *    camera pixel (row = y_corners[k] + i - 1, col = x_corners[k] + j - 1);
+ *  - outputs: params[k + P*roi] and crlb[k + P*roi] (Julia's results[k, idx],
+ *    uncertainties[k, idx]), llr[roi], flags[roi].
+ *  - parameter order per model: XYNB [x, y, N, bg]; XYNBS [x, y, N, bg, s];
+ *    XYNBSXSY [x, y, N, bg, sx, sy]; AstigmaticXYZNB [x, y, z, N, bg]
+ *    (src/psf_models.jl:20-24, 48-53, 74-80, 107-112). x, y are ROI pixels
+ *    (pixel centres at 1..box), sigmas in pixels, z in the units of gamma and d.
+ *
+ * Errors: every call returns a gmle_status; no exception or exit crosses the
+ * ABI; gmle_last_error() gives the message of the context's last failure.
+ * A per-ROI numerical failure is not an error: the ROI's CRLB is Inf and its
+ * GMLE_FLAG_CONVERGED bit is clear, as in src/unified_kernel.jl:424-430.
+ * There is no CPU fallback: without a usable GB300, gmle_create fails.
+ */
+#ifndef GAUSSMLE_GB300_H
+#define GAUSSMLE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GMLE_ABI_VERSION 1
+
+typedef enum {
+    GMLE_OK = 0,
+    GMLE_INVALID_ARG = 1,
+    GMLE_UNSUPPORTED_MODEL = 2,
+    GMLE_UNSUPPORTED_BOX = 3,
+    GMLE_OUT_OF_MEMORY = 4,
+    GMLE_ADMISSION_REJECTED = 5,
+    GMLE_CUDA_ERROR = 6,
+    GMLE_TIMEOUT = 7,
+    GMLE_NO_DEVICE = 8,
+    GMLE_NOT_READY = 9
+} gmle_status;
+
+/* PSF models, src/psf_models.jl:39-154 */
+typedef enum {
+    GMLE_MODEL_XYNB = 0,     /* GaussianXYNB: fixed sigma, P = 4 */
+    GMLE_MODEL_XYNBS = 1,    /* GaussianXYNBS: fitted sigma, P = 5 */
+    GMLE_MODEL_XYNBSXSY = 2, /* GaussianXYNBSXSY: fitted sigma_x, sigma_y, P = 6 */
+    GMLE_MODEL_ASTIG = 3     /* AstigmaticXYZNB: P = 5 */
+} gmle_model;
+
+/* Camera noise models, src/camera_models.jl:19-42 */
+typedef enum {
+    GMLE_CAMERA_POISSON = 0,   /* IdealCamera: Poisson likelihood */
+    GMLE_CAMERA_SCMOS = 1,     /* SCMOSCamera: data already in e-, variance map resident */
+    GMLE_CAMERA_SCMOS_ADU = 2  /* SCMOSCamera: data in ADU; e- = (ADU - offset) * gain
+                                  applied on the device (src/camera_models.jl:110-113) */
+} gmle_camera;
+
+/* Per-ROI output flag bits */
+#define GMLE_FLAG_CONVERGED 1u /* isfinite(CRLB_x): test/local_performance_benchmark.jl:291-293 */
+#define GMLE_FLAG_CHOLESKY 2u  /* Fisher inverse via Cholesky (src/unified_kernel.jl:412) */
+#define GMLE_FLAG_LU 4u        /* LU fallback (src/unified_kernel.jl:419) */
+#define GMLE_FLAG_SINGULAR 8u  /* both failed: CRLB = Inf (src/unified_kernel.jl:424-430) */
+
+/*
+ * Fit descriptor: the non-array arguments of unified_gaussian_mle_kernel!
+ * (src/unified_kernel.jl:286-297).
+ *  psf[]: model constants in PIXEL units (after to_pixel_units,
+ *         src/psf_models.jl:311-331): XYNB psf[0] = sigma; XYNBS, XYNBSXSY
+ *         unused; astigmatic psf = {sx0, sy0, Ax, Ay, Bx, By, gamma, d}.
+ *  lower/upper/max_step: ParameterConstraints (src/constraints.jl:5-9), first
+ *         P entries used.
+ */
+typedef struct {
+    int32_t model;      /* gmle_model */
+    int32_t box;        /* ROI edge length, 3..15 (kernels specialised for 7..15) */
+    int32_t iterations; /* Newton iterations (reference default 20) */
+    int32_t camera;     /* gmle_camera */
+    float psf[8];
+    float lower[6];
+    float upper[6];
+    float max_step[6];
+} gmle_fit_desc;
+
+typedef struct gmle_ctx gmle_ctx;
+
+/* Library ABI version (GMLE_ABI_VERSION). */
+int gmle_abi_version(void);
+
+/*
+ * Create a context on CUDA device `device_ordinal`: device selection replaces
+ * src/devices.jl:5-35 without its CPU fallback (returns GMLE_NO_DEVICE).
+ */
+gmle_status gmle_create(gmle_ctx **out, int device_ordinal);
+void gmle_destroy(gmle_ctx *ctx);
+const char *gmle_last_error(const gmle_ctx *ctx);
+
+/*
+ * Upload camera calibration maps once; they stay resident on the device and
+ * are used by every sCMOS fit of this context.  variance = readnoise^2 in e-^2
+ * (extract_variance_map, src/interface.jl:43-55); gain (e-/ADU) and offset
+ * (ADU) may be NULL when only GMLE_CAMERA_SCMOS fits are made.  Maps are
+ * (ny, nx) column-major.  Replaces the per-batch map upload of
+ * src/interface.jl:431-432.
+ */
+gmle_status gmle_set_calibration(gmle_ctx *ctx, const float *variance, const float *gain,
+                                 const float *offset, int32_t ny, int32_t nx);
+
+/*
+ * Synchronous fit of n ROIs from HOST memory into HOST memory: the whole GPU
+ * branch of fit (src/interface.jl:220-262 and its ROIBatch twins).  Pinned
+ * caller buffers are copied by DMA directly; pageable ones are staged through
+ * the context's pinned buffers.  Transfers of one chunk overlap the fit of
+ * the previous one.  x_corners / y_corners may be NULL for Poisson fits;
+ * flags may be NULL.
+ */
+gmle_status gmle_fit(gmle_ctx *ctx, const gmle_fit_desc *desc, const float *data,
+                     const int32_t *x_corners, const int32_t *y_corners, int64_t n,
+                     float *params, float *crlb, float *llr, uint8_t *flags);
+
+/*
+ * Asynchronous fit of n ROIs already resident in DEVICE memory (for callers
+ * that hold device arrays, e.g. a CuArray): enqueues the fit kernel on
+ * `stream` (a cudaStream_t; NULL = the context's stream) and returns.  All
+ * pointers are device pointers; flags may be NULL.  Corners outside the
+ * calibration map are reported through gmle_fit_device_errors().
+ */
+gmle_status gmle_fit_device(gmle_ctx *ctx, const gmle_fit_desc *desc, const float *d_data,
+                            const int32_t *d_x_corners, const int32_t *d_y_corners, int64_t n,
+                            float *d_params, float *d_crlb, float *d_llr, uint8_t *d_flags,
+                            void *stream);
+
+/* Number of ROIs rejected by device-side corner checks since the last call
+ * (synchronises the context's stream). */
+gmle_status gmle_fit_device_errors(gmle_ctx *ctx, int64_t *count);
+
+/*
+ * Kernel launch shape used for a (model, box, camera): threads per ROI and
+ * ROIs per block, as picked by the autotuner (or set by gmle_set_tuning).
+ */
+gmle_status gmle_get_tuning(gmle_ctx *ctx, int32_t model, int32_t box, int32_t camera,
+                            int32_t *threads_per_roi, int32_t *rois_per_block);
+gmle_status gmle_set_tuning(gmle_ctx *ctx, int32_t model, int32_t box, int32_t camera,
+                            int32_t threads_per_roi, int32_t rois_per_block);
+
+/* Number of fit-kernel launches this context has issued (for accounting). */
+int64_t gmle_kernel_launches(const gmle_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GAUSSMLE_GB300_H */
