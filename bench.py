@@ -52,6 +52,8 @@ def parse():
                    help="target CPU time of the cpu_baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--shape", default=None,
+                   help="THREADS_PER_ROI,ROIS_PER_BLOCK: fixed launch shape instead of autotuning")
     return p.parse_args()
 
 
@@ -254,15 +256,33 @@ def run_ours(args):
     crlb = torch.empty((n, P), device=dev)
     llr = torch.empty(n, device=dev)
     flags = torch.empty(n, dtype=torch.uint8, device=dev)
-    stream = torch.cuda.current_stream(dev)
+    stream = torch.cuda.Stream(dev)   # the launch stream; events are recorded on it
 
     def step():
         G.fit_device(ctx, desc, wl["data"], wl["xc"], wl["yc"], params, crlb, llr, flags,
                      stream=stream)
 
+    # launch shape chosen by the project's autotuner (untimed), or fixed by --shape
+    from gaussmle_gb300 import tuning
+    if args.shape:
+        tpr, rpb = (int(v) for v in args.shape.split(","))
+        ctx.check(ctx.lib.gmle_set_tuning(ctx.handle, 1, 13, 2, tpr, rpb))
+        tune = (tpr, rpb, None)
+    else:
+        tune = tuning.autotune(ctx, desc, wl["data"], wl["xc"], wl["yc"], params, crlb, llr,
+                               flags, save=False)
+
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
+    # time of one launch alone (for the roofline; same stream, events around it)
+    a0 = torch.cuda.Event(enable_timing=True)
+    a1 = torch.cuda.Event(enable_timing=True)
+    a0.record(stream)
+    step()
+    a1.record(stream)
+    torch.cuda.synchronize()
+    single_launch_s = a0.elapsed_time(a1) / 1e3
     launches0 = ctx.launches()
     sampler = ClockSampler(local)
     sampler.start()
@@ -327,7 +347,7 @@ def run_ours(args):
     # ---- roofline: issue-bound FP32 + SFU work vs the measured FP32 rate ----
     w = roofline.work_per_roi(1, 13, 20, 2)
     peak_inst = fp32_peak_tinst(torch, dev)  # T lane-inst/s
-    achieved = w["fp32_equiv"] * n / per_launch / 1e12
+    achieved = w["fp32_equiv"] * n / per_launch / 1e12  # per launch, averaged over the K steps
     peaks = measured_peaks()
     bpr = roofline.bytes_per_roi(1, 13, 2)
     hbm_ach = bpr * n / per_launch / 1e9
@@ -335,7 +355,7 @@ def run_ours(args):
         "bound": "fp32+sfu", "achieved": achieved, "peak": peak_inst, "unit": "Tinst/s",
         "frac": achieved / peak_inst, "traffic": None,
         "peak_source": "measured in this run: FP32 SGEMM 8192^3 (TF32 off) FFMA rate",
-        "work_per_roi_fp32_equiv": w["fp32_equiv"],
+        "work_per_roi_fp32_equiv": w["fp32_equiv"], "single_launch_ms": single_launch_s * 1e3,
         "hbm": {"achieved_gbs": hbm_ach, "peak_gbs": peaks.get("hbm_gbs"),
                 "frac": hbm_ach / peaks.get("hbm_gbs", 6800.0), "bytes_per_roi": bpr,
                 "peak_source": "MEASURED_PEAKS.json" if "source" not in peaks else "fallback"},
@@ -350,7 +370,8 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "rois_per_step": n, "box": 13, "model": "GaussianXYNBS",
                    "camera": "sCMOS (ADU, device-side conversion)", "iterations": 20,
                    "parallelism": f"roi-shard x{world}", "l2": "inputs (676 MB/step) > L2",
-                   "tuning": list(G_tuning(ctx))},
+                   "tuning": {"threads_per_roi": tune[0], "rois_per_block": tune[1],
+                              "source": "--shape" if args.shape else "gmle_autotune"}},
         "gpu_launches": launches,
         "converged_fraction": conv,
         "clocks": clocks,
@@ -359,12 +380,6 @@ def run_ours(args):
         "cpu_baseline": cpu,
     }
     print(json.dumps(out))
-
-
-def G_tuning(ctx):
-    a, b = C.c_int32(), C.c_int32()
-    ctx.lib.gmle_get_tuning(ctx.handle, 1, 13, 2, C.byref(a), C.byref(b))
-    return a.value, b.value
 
 
 def main():

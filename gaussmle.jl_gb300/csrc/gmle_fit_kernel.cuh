@@ -11,12 +11,12 @@
 //    the Julia (box, box, n) layout; it stages them into shared memory with
 //    coalesced 16-byte loads (plus the sCMOS variance tile gathered from the
 //    resident calibration map, with the ADU->e- conversion fused in).
-//  * `tpr` lanes (1..32, a power of two) fit one ROI; lane r owns pixel
-//    columns j = r+1, r+1+tpr, ...  Per Newton iteration the model is
-//    separable: per axis the erf/exp terms are evaluated once per pixel index
-//    (box entries per axis instead of box^2 per pixel), the y-axis tables are
-//    shared through shared memory and held in registers, and each pixel costs
-//    a few FP32 FMAs.
+//  * `tpr` lanes (1..32, a power of two) fit one ROI; lane r owns a
+//    contiguous block of pixel columns.  Per Newton iteration the model is
+//    separable: per axis the erf/exp terms are evaluated once per pixel edge
+//    (box + 1 per axis instead of 4 per pixel), the y-axis tables are shared
+//    through shared memory and held in registers, and per pixel only the
+//    likelihood terms are formed and summed into per-column and per-row sums.
 //  * Gradient and diagonal Hessian are summed with warp shuffles; every lane
 //    of the group then applies the same Newton step, so theta stays identical.
 //  * Final pass: FP32 per-pixel Fisher products, summed per column in FP32
@@ -97,6 +97,7 @@ __device__ __forceinline__ float jl_pow5f(float x)
 struct Axis {
     float c;     // centre (x or y, ROI pixels)
     float s;     // sigma (pixels)
+    float inv_s; // 1 / s
     float sq;    // sqrt(0.5 / s^2): integral_gaussian_1d, baselibrary.jl:8-14
     float cst;   // (-N / sqrt(2pi)) / s: derivative_integral_gaussian_1d, baselibrary.jl:21-33
     float cst2;  // cst / s^2
@@ -107,47 +108,84 @@ struct Axis {
 
 __device__ __forceinline__ Axis make_axis(float c, float s, float N, float sqrt2pi, bool sig)
 {
+    // One division per axis; the remaining factors are products of 1/s, each
+    // within a few ulp of the reference's chained divisions.
     Axis a;
     a.c = c;
     a.s = s;
-    float s2 = __fmul_rn(s, s);
-    a.sq = sqrtf(__fdiv_rn(0.5f, s2));
-    float nk = __fdiv_rn(-N, sqrt2pi);
-    a.cst = __fdiv_rn(nk, s);
-    a.cst2 = __fdiv_rn(a.cst, s2);
+    const float is = __fdiv_rn(1.0f, s);
+    a.inv_s = is;
+    const float is2 = is * is;
+    a.sq = 0.70710678118654752f * is;                 // sqrt(1/2 / s^2), s > 0
+    const float nk = -N * __fdiv_rn(1.0f, sqrt2pi);   // -N / sqrt(2 pi)
+    a.cst = nk * is;
+    a.cst2 = a.cst * is2;
     if (sig) {
-        a.s1c = __fdiv_rn(a.cst, s);
-        a.s2c = __fdiv_rn(__fdiv_rn(N, sqrt2pi), jl_pow5f(s));
-        a.m2s = __fdiv_rn(-2.0f, s);
+        a.s1c = a.cst * is;
+        a.s2c = -nk * (is2 * is2 * is);
+        a.m2s = -2.0f * is;
     } else {
         a.s1c = a.s2c = a.m2s = 0.f;
     }
     return a;
 }
 
-// Per-axis table entry at pixel index t (1-based).  psf: integral_gaussian_1d;
-// d1, d2: derivative_integral_gaussian_1d without the PSF-of-the-other-axis
-// factor; s1, s2: derivative_integral_gaussian_1d_sigma likewise.  The
-// expressions keep the reference's association: (t - c) + 1/2 inside erf and
-// the sigma products, (t + 1/2) - c inside exp.
+// Table entries of consecutive pixel indices along one axis.  Neighbouring
+// pixels share an edge: the exp at the upper edge of pixel t is the exp at the
+// lower edge of pixel t+1 (both arguments are the same float, (t + 1/2) - c),
+// and the erf at the upper edge, ((t - c) + 1/2) * sq, is reused as the lower
+// edge of t+1, ((t + 1 - c) - 1/2) * sq, whenever the two arguments are equal
+// (always, unless t - c rounds; then the lower edge is evaluated).  A run of
+// pixels costs about one erf and one exp per pixel instead of two of each.
+struct EdgeWalk {
+    float ua;    // erf-argument offset (t - c) + 1/2 of the previous pixel's upper edge
+    float erfa;  // erf(ua * sq)
+    float fa;    // exp at the previous pixel's upper edge
+};
+
+// Start a walk at pixel t0: the values of its lower edge.
+__device__ __forceinline__ EdgeWalk walk_start(int t0, const Axis &a)
+{
+    const float tf = (float)t0;
+    const float ub = __fadd_rn(tf - a.c, -0.5f);
+    const float tb = (__fadd_rn(tf, -0.5f) - a.c) * a.inv_s;
+    EdgeWalk w;
+    w.ua = ub;
+    w.erfa = erff(__fmul_rn(ub, a.sq));
+    w.fa = expf(-0.5f * __fmul_rn(tb, tb));
+    return w;
+}
+
+// psf: integral_gaussian_1d (baselibrary.jl:8-14); d1, d2:
+// derivative_integral_gaussian_1d (baselibrary.jl:21-33) and s1, s2:
+// derivative_integral_gaussian_1d_sigma (baselibrary.jl:40-52), each without
+// the factor PSF of the other axis.  The expressions keep the reference's
+// association: (t - c) + 1/2 inside erf and the sigma products, (t + 1/2) - c
+// inside exp.
 template <bool SIG, bool SECOND>
-__device__ __forceinline__ void axis_entry(int t, const Axis &a, float &psf, float &d1, float &d2,
-                                           float &s1, float &s2)
+__device__ __forceinline__ void walk_entry(int t, const Axis &a, EdgeWalk &w, float &psf,
+                                           float &d1, float &d2, float &s1, float &s2)
 {
     const float tf = (float)t;
     const float tc = tf - a.c;
     const float ua = __fadd_rn(tc, 0.5f), ub = __fadd_rn(tc, -0.5f);
-    psf = 0.5f * (erff(__fmul_rn(ua, a.sq)) - erff(__fmul_rn(ub, a.sq)));
+    float erfb = w.erfa;
+    if (ub != w.ua) erfb = erff(__fmul_rn(ub, a.sq));
+    const float erfa = erff(__fmul_rn(ua, a.sq));
+    psf = 0.5f * (erfa - erfb);
     const float ea = __fadd_rn(tf, 0.5f) - a.c, eb = __fadd_rn(tf, -0.5f) - a.c;
-    const float ta = __fdiv_rn(ea, a.s), tb = __fdiv_rn(eb, a.s);
+    const float fb = w.fa;
+    const float ta = ea * a.inv_s;
     const float fa = expf(-0.5f * __fmul_rn(ta, ta));
-    const float fb = expf(-0.5f * __fmul_rn(tb, tb));
     d1 = a.cst * (fa - fb);
     if (SECOND) d2 = a.cst2 * (ea * fa - eb * fb);
     if (SIG) {
         s1 = a.s1c * (fa * ua - fb * ub);
         if (SECOND) s2 = a.s2c * (fa * (ua * ua * ua) - fb * (ub * ub * ub));
     }
+    w.ua = ua;
+    w.erfa = erfa;
+    w.fa = fa;
 }
 
 // Astigmatic width model, src/psf_derivatives.jl:118-163 (per iteration, scalar).
@@ -209,22 +247,24 @@ __device__ __forceinline__ double group_sum(double v, int tpr)
 // ---- initialisation, src/unified_kernel.jl:158-255 (one lane, reference order,
 // no FMA contraction so that the start point matches the FP32 reference) ----
 
-template <int MODEL, int BOX>
-__device__ void initialize(const float *roi, const float *psf, float *th)
+template <int MODEL, int BOX, int STRIDE>
+__device__ void initialize(const float *roi_pix, const float *psf, float *th)
 {
+    // roi_pix holds the ROI's pixels STRIDE floats apart (2: (data, variance) pairs)
+    auto roi = [&](int p) { return roi_pix[STRIDE * p]; };
     float edge_sum = 0.f;
     int edge_count = 0;
     for (int j = 1; j <= BOX; j++)
         for (int i = 1; i <= BOX; i++)
             if (i == 1 || i == BOX || j == 1 || j == BOX) {
-                edge_sum = __fadd_rn(edge_sum, roi[(i - 1) + BOX * (j - 1)]);
+                edge_sum = __fadd_rn(edge_sum, roi((i - 1) + BOX * (j - 1)));
                 edge_count++;
             }
     const float bg = __fdiv_rn(edge_sum, (float)edge_count);
     float total = 0.f, xw = 0.f, yw = 0.f;
     for (int j = 1; j <= BOX; j++)
         for (int i = 1; i <= BOX; i++) {
-            const float sig = jl_maxf(0.f, __fadd_rn(roi[(i - 1) + BOX * (j - 1)], -bg));
+            const float sig = jl_maxf(0.f, __fadd_rn(roi((i - 1) + BOX * (j - 1)), -bg));
             total = __fadd_rn(total, sig);
             xw = __fadd_rn(xw, __fmul_rn(sig, (float)j));
             yw = __fadd_rn(yw, __fmul_rn(sig, (float)i));
@@ -242,7 +282,7 @@ __device__ void initialize(const float *roi, const float *psf, float *th)
         float tot2 = 0.f, mxx = 0.f, myy = 0.f;
         for (int j = 1; j <= BOX; j++)
             for (int i = 1; i <= BOX; i++) {
-                const float sig = jl_maxf(0.f, __fadd_rn(roi[(i - 1) + BOX * (j - 1)], -bg));
+                const float sig = jl_maxf(0.f, __fadd_rn(roi((i - 1) + BOX * (j - 1)), -bg));
                 tot2 = __fadd_rn(tot2, sig);
                 const float dx = __fadd_rn((float)j, -x), dy = __fadd_rn((float)i, -y);
                 mxx = __fadd_rn(mxx, __fmul_rn(__fmul_rn(sig, dx), dx));
@@ -374,10 +414,12 @@ __device__ uint8_t crlb_from_fisher(double (&F)[P][P], float *crlb)
     return flags;
 }
 
-// ---- the kernel ---------------------------------------------------------------
 
-// Shared memory per ROI slot: [BOX^2 data][BOX^2 variance if SCMOS][ok flag]
-// [NT * BOX y-tables, only when tpr > 1], laid out as arrays over the R slots.
+// ---- shared pieces of the two kernels ----------------------------------------
+
+// Shared memory, as arrays over the R ROI slots of a block: pixels (float, or
+// float2 (data in e-, read-noise variance) for sCMOS), one ok flag per slot,
+// and, when several lanes share a ROI (tpr > 1), NT * BOX y-axis table entries.
 inline size_t smem_bytes(int model, int box, bool scmos, int tpr, int rois)
 {
     const int nt = model == 0 ? 3 : 5;
@@ -386,297 +428,594 @@ inline size_t smem_bytes(int model, int box, bool scmos, int tpr, int rois)
                            sizeof(int));
 }
 
+// Stage the block's R ROIs (contiguous in global memory) into shared memory;
+// for sCMOS gather the variance tile from the resident map and apply the
+// ADU -> e- conversion of src/camera_models.jl:110-113 on the way.
+template <int BOX, bool SCMOS>
+__device__ __forceinline__ void stage_block(const KernelArgs &a, float *spix, int *sok, int R,
+                                            int64_t roi0, int nroi)
+{
+    constexpr int B2 = BOX * BOX;
+    for (int g = threadIdx.x; g < R; g += blockDim.x) {
+        int ok = g < nroi;
+        if (SCMOS && ok) {
+            const int32_t x0 = a.xc[roi0 + g], y0 = a.yc[roi0 + g];
+            ok = x0 >= 1 && y0 >= 1 && x0 + BOX - 1 <= a.nx && y0 + BOX - 1 <= a.ny;
+            if (!ok) atomicAdd(a.bad_corners, 1ull);
+        }
+        sok[g] = ok;
+    }
+    const float *src = a.data + roi0 * B2;
+    const int cnt = nroi * B2;
+    if (!SCMOS) {
+        if ((reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
+            const int c4 = cnt >> 2;
+            const float4 *s4 = reinterpret_cast<const float4 *>(src);
+            float4 *d4 = reinterpret_cast<float4 *>(spix);
+            for (int e = threadIdx.x; e < c4; e += blockDim.x) d4[e] = __ldg(s4 + e);
+            for (int e = (c4 << 2) + threadIdx.x; e < cnt; e += blockDim.x) spix[e] = __ldg(src + e);
+        } else {
+            for (int e = threadIdx.x; e < cnt; e += blockDim.x) spix[e] = __ldg(src + e);
+        }
+        for (int e = cnt + threadIdx.x; e < R * B2; e += blockDim.x) spix[e] = 0.f;
+    } else {
+        __syncthreads();  // sok
+        // consecutive e walk down a column: contiguous map addresses
+        float2 *s2 = reinterpret_cast<float2 *>(spix);
+        for (int e = threadIdx.x; e < R * B2; e += blockDim.x) {
+            const int g = e / B2;
+            float2 v = make_float2(0.f, 0.f);
+            if (e < cnt) {
+                v.x = __ldg(src + e);
+                if (sok[g]) {
+                    const int p = e - g * B2, j = p / BOX, i = p - j * BOX;
+                    const int64_t m = (int64_t)(a.yc[roi0 + g] - 1 + i) +
+                                      (int64_t)a.ny * (int64_t)(a.xc[roi0 + g] - 1 + j);
+                    if (a.adu) v.x = __fmul_rn(__fadd_rn(v.x, -__ldg(a.offset + m)), __ldg(a.gain + m));
+                    v.y = __ldg(a.var + m);
+                }
+            }
+            s2[e] = v;
+        }
+    }
+    __syncthreads();
+}
+
+template <int MODEL> struct Slots {
+    static constexpr int IX = 0, IY = 1;
+    static constexpr int IN = (MODEL == 3) ? 3 : 2;
+    static constexpr int IB = (MODEL == 3) ? 4 : 3;
+};
+
+// Likelihood terms of one pixel: compute_likelihood_terms, Poisson
+// src/camera_models.jl:19-34 and sCMOS :36-42 (1/x by __fdividef, 2 ulp).
+template <bool SCMOS>
+__device__ __forceinline__ void likelihood_terms(float d, float v, float mu, float &cf, float &df)
+{
+    if (!SCMOS) {
+        const float rm = __fdividef(1.0f, mu);
+        const float q = d * rm;
+        const bool pos = mu > 0.01f;
+        cf = pos ? fminf(q - 1.0f, 1e4f) : 0.f;
+        df = pos ? fminf(q * rm, 1e4f) : 0.f;
+    } else {
+        const float rv = __fdividef(1.0f, mu + v);
+        cf = (d - mu) * rv;
+        df = rv;
+    }
+}
+
+// Column-side contributions to gradient gs and diagonal Hessian hs of one pixel
+// column j with x-table entry (xp, xd1, xd2, xs1, xs2) and the column sums
+// A = sum_i py cf, B = sum_i py^2 df, E = sum_i cf, F = sum_i df,
+// G = sum_i py ys1 df (dudt and d2udt2 as in src/psf_derivatives.jl).
+template <int MODEL, int P>
+__device__ __forceinline__ void col_terms(float (&gs)[P], float (&hs)[P], float xp, float xd1,
+                                          float xd2, float xs1, float xs2, float A, float B,
+                                          float E, float F, float Gc, const Axis &ax,
+                                          const AstigWidths &aw)
+{
+    using S = Slots<MODEL>;
+    gs[S::IX] = fmaf(xd1, A, gs[S::IX]);
+    hs[S::IX] += xd2 * A - xd1 * xd1 * B;
+    gs[S::IN] = fmaf(xp, A, gs[S::IN]);
+    hs[S::IN] -= xp * xp * B;
+    gs[S::IB] += E;
+    hs[S::IB] -= F;
+    if (MODEL == 1) {
+        gs[4] = fmaf(xs1, A, gs[4]);
+        hs[4] += (ax.m2s * xs1 - xs2) * A - xs1 * xs1 * B - 2.0f * xs1 * xp * Gc;
+    } else if (MODEL == 2) {
+        gs[4] = fmaf(xs1, A, gs[4]);
+        hs[4] += (ax.m2s * xs1 - xs2) * A - xs1 * xs1 * B;
+    } else if (MODEL == 3) {
+        const float c1 = xs1 * aw.dsx;
+        gs[2] = fmaf(c1, A, gs[2]);
+        hs[2] += ((ax.m2s * xs1 - xs2) * (aw.dsx * aw.dsx) + xs1 * aw.d2sx) * A - c1 * c1 * B -
+                 2.0f * c1 * (xp * aw.dsy) * Gc;
+    }
+}
+
+// Row-side contributions of pixel row t: y-table entry (yd1, yd2, ys1, ys2) and
+// the row sums C = sum_j xp cf, D = sum_j xp^2 df.
+template <int MODEL, int P>
+__device__ __forceinline__ void row_terms(float (&gs)[P], float (&hs)[P], float yd1, float yd2,
+                                          float ys1, float ys2, float Ct, float Dt,
+                                          const Axis &ay, const AstigWidths &aw)
+{
+    gs[1] = fmaf(yd1, Ct, gs[1]);
+    hs[1] += yd2 * Ct - yd1 * yd1 * Dt;
+    if (MODEL == 1) {
+        gs[4] = fmaf(ys1, Ct, gs[4]);
+        hs[4] += (ay.m2s * ys1 - ys2) * Ct - ys1 * ys1 * Dt;
+    } else if (MODEL == 2) {
+        gs[5] = fmaf(ys1, Ct, gs[5]);
+        hs[5] += (ay.m2s * ys1 - ys2) * Ct - ys1 * ys1 * Dt;
+    } else if (MODEL == 3) {
+        const float c2 = ys1 * aw.dsy;
+        gs[2] = fmaf(c2, Ct, gs[2]);
+        hs[2] += ((ay.m2s * ys1 - ys2) * (aw.dsy * aw.dsy) + ys1 * aw.d2sy) * Ct - c2 * c2 * Dt;
+    }
+}
+
+// Scalar Newton step, src/unified_kernel.jl:337-350, with apply_constraints!,
+// src/constraints.jl:49-53.
+template <int P>
+__device__ __forceinline__ void newton_step(float (&th)[P], const float (&gs)[P],
+                                            const float (&hs)[P], const KernelArgs &a)
+{
+#pragma unroll
+    for (int k = 0; k < P; k++) {
+        const float delta = fabsf(hs[k]) > 1e-10f ? __fdiv_rn(gs[k], hs[k]) : 0.f;
+        const float step = jl_clamp(delta, -a.max_step[k], a.max_step[k]);
+        th[k] = jl_clamp(__fadd_rn(th[k], -step), a.lower[k], a.upper[k]);
+    }
+}
+
+// Separable structure of dudt_k = sum_t a_kt(j) * b_kt(i): each parameter has
+// one or two terms, each a column function a (x-axis tables) times a row
+// function b, with b in {0: psf_y, 1: d psf_y/dy, 2: 1, 3: d psf_y/dsigma_y}.
+__host__ __device__ constexpr int term_count(int model, int k)
+{
+    return ((model == 1 && k == 4) || (model == 3 && k == 2)) ? 2 : 1;
+}
+__host__ __device__ constexpr int term_b(int model, int k, int t)
+{
+    // parameter slots: x 0, y 1; N, bg at 2, 3 (3, 4 for the astigmatic model)
+    return model == 3 ? (k == 0 ? 0 : k == 1 ? 1 : k == 2 ? (t == 0 ? 0 : 3) : k == 3 ? 0 : 2)
+                      : (k == 0 ? 0 : k == 1 ? 1 : k == 2 ? 0 : k == 3 ? 2
+                                                   : k == 4 ? (model == 1 ? (t == 0 ? 0 : 3) : 0)
+                                                            : 3);
+}
+
+template <int NB>
+__device__ __forceinline__ float qsym(const float (&Q)[NB][NB], int p, int q)
+{
+    return p <= q ? Q[p][q] : Q[q][p];
+}
+
+// Per pixel of the final pass: the LLR term (compute_log_likelihood,
+// src/camera_models.jl:60-96) and the Fisher weight sums Q_pq += b_p b_q w,
+// w = 1/variance over pixels with mu > 0 (src/unified_kernel.jl:378-396).
+template <bool SCMOS, bool SIG, int NB>
+__device__ __forceinline__ void final_pixel(float d, float v, float mu, float py, float yd1,
+                                            float ys1, float &llr, float (&Q)[NB][NB])
+{
+    if (!SCMOS) {
+        if (mu > 0.f && d > 0.f)
+            llr += d * logf(mu) - mu - (d * logf(d) - d);
+        else if (mu > 0.f && d == 0.f)
+            llr -= mu;
+    } else {
+        const float tv = mu + v;
+        if (tv > 0.f) {
+            const float res = d - mu;
+            llr += -0.5f * __fdiv_rn(res * res, tv);
+        }
+    }
+    const float w = mu > 0.f ? __fdividef(1.0f, SCMOS ? mu + v : mu) : 0.f;
+    const float t0 = py * w, t1 = yd1 * w;
+    Q[0][0] = fmaf(t0, py, Q[0][0]);
+    Q[0][1] = fmaf(t0, yd1, Q[0][1]);
+    Q[0][2] += t0;
+    Q[1][1] = fmaf(t1, yd1, Q[1][1]);
+    Q[1][2] += t1;
+    Q[2][2] += w;
+    if (SIG) {
+        const float t3 = ys1 * w;
+        Q[0][3] = fmaf(t0, ys1, Q[0][3]);
+        Q[1][3] = fmaf(t1, ys1, Q[1][3]);
+        Q[2][3] += t3;
+        Q[3][3] = fmaf(t3, ys1, Q[3][3]);
+    }
+}
+
+// One column's Fisher contribution: F_kl += sum_{t,u} a_kt a_lu Q[b_kt][b_lu],
+// summed in FP32 for the column and accumulated in FP64.
+template <int MODEL, int P, int NB>
+__device__ __forceinline__ void fisher_column(double (&Fm)[P][P], const float (&Q)[NB][NB],
+                                              float xp, float xd1, float xs1,
+                                              const AstigWidths &aw)
+{
+    using S = Slots<MODEL>;
+    float av[P][2];
+    av[S::IX][0] = xd1; av[S::IX][1] = 0.f;
+    av[S::IY][0] = xp;  av[S::IY][1] = 0.f;
+    av[S::IN][0] = xp;  av[S::IN][1] = 0.f;
+    av[S::IB][0] = 1.f; av[S::IB][1] = 0.f;
+    if (MODEL == 1) { av[4][0] = xs1; av[4][1] = xp; }
+    if (MODEL == 2) { av[4][0] = xs1; av[4][1] = 0.f; av[5][0] = xp; av[5][1] = 0.f; }
+    if (MODEL == 3) { av[2][0] = xs1 * aw.dsx; av[2][1] = xp * aw.dsy; }
+#pragma unroll
+    for (int k = 0; k < P; k++)
+#pragma unroll
+        for (int l = k; l < P; l++) {
+            float s = 0.f;
+#pragma unroll
+            for (int tk = 0; tk < term_count(MODEL, k); tk++)
+#pragma unroll
+                for (int tl = 0; tl < term_count(MODEL, l); tl++)
+                    s = fmaf(av[k][tk] * av[l][tl],
+                             qsym<NB>(Q, term_b(MODEL, k, tk), term_b(MODEL, l, tl)), s);
+            Fm[k][l] += (double)s;
+        }
+}
+
+template <int P>
+__device__ __forceinline__ void write_result(const KernelArgs &a, int64_t roi, bool valid,
+                                             const float (&th)[P], double (&Fm)[P][P], float llr)
+{
+    if (valid) {
+        float cr[P];
+        const uint8_t fl = crlb_from_fisher<P>(Fm, cr);
+#pragma unroll
+        for (int k = 0; k < P; k++) {
+            a.params[roi * P + k] = th[k];
+            a.crlb[roi * P + k] = cr[k];
+        }
+        a.llr[roi] = llr;
+        if (a.flags) a.flags[roi] = fl;
+    } else {
+        // corner outside the calibration map: no fit
+        const float qnan = __int_as_float(0x7fc00000);
+#pragma unroll
+        for (int k = 0; k < P; k++) { a.params[roi * P + k] = qnan; a.crlb[roi * P + k] = qnan; }
+        a.llr[roi] = qnan;
+        if (a.flags) a.flags[roi] = 0;
+    }
+}
+
+template <int MODEL>
+__device__ __forceinline__ void axis_widths(const float *th, const KernelArgs &a, float &sxw,
+                                            float &syw, AstigWidths &aw)
+{
+    if (MODEL == 0) { sxw = syw = a.psf[0]; }
+    else if (MODEL == 1) { sxw = syw = th[4]; }
+    else if (MODEL == 2) { sxw = th[4]; syw = th[5]; }
+    else { astig_widths(th[2], a.psf, aw); sxw = aw.sx; syw = aw.sy; }
+}
+
+// ---- kernel 1: one thread per ROI ---------------------------------------------
+//
+// Each thread fits one ROI with every axis table in registers; per column the
+// next column's erf/exp evaluations are issued before the current column's
+// pixel work so that their latency overlaps it.  Occupancy is bounded by
+// shared memory (the staged pixels), so registers are not the constraint.
+template <int MODEL, int BOX, bool SCMOS>
+__global__ void __launch_bounds__(64) fit_kernel_r1(const KernelArgs a)
+{
+    constexpr int P = ModelInfo<MODEL>::P;
+    constexpr bool SIG = ModelInfo<MODEL>::SIG;
+    constexpr bool CROSS = (MODEL == 1 || MODEL == 3);
+    constexpr int B2 = BOX * BOX;
+    constexpr int PS = SCMOS ? 2 : 1;
+    constexpr int NB = SIG ? 4 : 3;
+    using S = Slots<MODEL>;
+
+    extern __shared__ __align__(16) float smem[];
+    const int R = blockDim.x;
+    float *spix = smem;
+    int *sok = reinterpret_cast<int *>(spix + R * B2 * PS);
+    const int64_t roi0 = (int64_t)blockIdx.x * R;
+    const int64_t left = a.n - roi0;
+    const int nroi = left < R ? (int)left : R;
+    stage_block<BOX, SCMOS>(a, spix, sok, R, roi0, nroi);
+
+    const int g = threadIdx.x;
+    if (__all_sync(0xffffffffu, g >= nroi)) return;
+    const bool valid = g < nroi && sok[g];
+    const float *pix = spix + g * B2 * PS;
+
+    float th[P];
+#pragma unroll
+    for (int k = 0; k < P; k++) th[k] = 0.f;
+    initialize<MODEL, BOX, PS>(pix, a.psf, th);
+
+    float py[BOX], yd1[BOX], yd2[BOX], ys1[SIG ? BOX : 1], ys2[SIG ? BOX : 1];
+    for (int it = 0; it <= a.iterations; ++it) {
+        const bool final_pass = (it == a.iterations);
+        float sxw, syw;
+        AstigWidths aw;
+        axis_widths<MODEL>(th, a, sxw, syw, aw);
+        const float N = th[S::IN], bg = th[S::IB];
+        const Axis ax = make_axis(th[S::IX], sxw, N, a.sqrt2pi, SIG);
+        const Axis ay = make_axis(th[S::IY], syw, N, a.sqrt2pi, SIG);
+        {
+            EdgeWalk wy = walk_start(1, ay);
+#pragma unroll
+            for (int t = 0; t < BOX; t++) {
+                float s1 = 0.f, s2 = 0.f;
+                walk_entry<SIG, true>(t + 1, ay, wy, py[t], yd1[t], yd2[t], s1, s2);
+                if (SIG) { ys1[t] = s1; ys2[t] = s2; }
+            }
+        }
+        EdgeWalk wx = walk_start(1, ax);
+        float xp, xd1, xd2, xs1 = 0.f, xs2 = 0.f;
+        walk_entry<SIG, true>(1, ax, wx, xp, xd1, xd2, xs1, xs2);
+
+        if (!final_pass) {
+            float py2[BOX], aG[CROSS ? BOX : 1], C[BOX], D[BOX];
+#pragma unroll
+            for (int t = 0; t < BOX; t++) {
+                py2[t] = py[t] * py[t];
+                if (CROSS) aG[t] = py[t] * ys1[t];
+                C[t] = 0.f;
+                D[t] = 0.f;
+            }
+            float gs[P], hs[P];
+#pragma unroll
+            for (int k = 0; k < P; k++) { gs[k] = 0.f; hs[k] = 0.f; }
+            for (int j = 1; j <= BOX; j++) {
+                // next column's table entry: independent of this column's pixels
+                float nxp, nxd1, nxd2, nxs1 = 0.f, nxs2 = 0.f;
+                walk_entry<SIG, true>(j + 1, ax, wx, nxp, nxd1, nxd2, nxs1, nxs2);
+                const float npx = N * xp, xp2 = xp * xp;
+                const float *col = pix + (j - 1) * BOX * PS;
+                float A = 0.f, B = 0.f, E = 0.f, F = 0.f, Gc = 0.f;
+#pragma unroll
+                for (int t = 0; t < BOX; t++) {
+                    float d, v = 0.f;
+                    if (SCMOS) {
+                        const float2 q = reinterpret_cast<const float2 *>(col)[t];
+                        d = q.x; v = q.y;
+                    } else {
+                        d = col[t];
+                    }
+                    const float mu = fmaf(npx, py[t], bg);
+                    float cf, df;
+                    likelihood_terms<SCMOS>(d, v, mu, cf, df);
+                    A = fmaf(py[t], cf, A);
+                    B = fmaf(py2[t], df, B);
+                    E += cf;
+                    F += df;
+                    C[t] = fmaf(xp, cf, C[t]);
+                    D[t] = fmaf(xp2, df, D[t]);
+                    if (CROSS) Gc = fmaf(aG[t], df, Gc);
+                }
+                col_terms<MODEL, P>(gs, hs, xp, xd1, xd2, xs1, xs2, A, B, E, F, Gc, ax, aw);
+                xp = nxp; xd1 = nxd1; xd2 = nxd2; xs1 = nxs1; xs2 = nxs2;
+            }
+#pragma unroll
+            for (int t = 0; t < BOX; t++)
+                row_terms<MODEL, P>(gs, hs, yd1[t], yd2[t], SIG ? ys1[t] : 0.f,
+                                    SIG ? ys2[t] : 0.f, C[t], D[t], ay, aw);
+            newton_step<P>(th, gs, hs, a);
+        } else {
+            float llr = 0.f;
+            double Fm[P][P];
+#pragma unroll
+            for (int k = 0; k < P; k++)
+#pragma unroll
+                for (int l = 0; l < P; l++) Fm[k][l] = 0.0;
+            for (int j = 1; j <= BOX; j++) {
+                float nxp, nxd1, nxd2, nxs1 = 0.f, nxs2 = 0.f;
+                walk_entry<SIG, false>(j + 1, ax, wx, nxp, nxd1, nxd2, nxs1, nxs2);
+                const float npx = N * xp;
+                const float *col = pix + (j - 1) * BOX * PS;
+                float Q[NB][NB];
+#pragma unroll
+                for (int p = 0; p < NB; p++)
+#pragma unroll
+                    for (int q = 0; q < NB; q++) Q[p][q] = 0.f;
+#pragma unroll
+                for (int t = 0; t < BOX; t++) {
+                    float d, v = 0.f;
+                    if (SCMOS) {
+                        const float2 q = reinterpret_cast<const float2 *>(col)[t];
+                        d = q.x; v = q.y;
+                    } else {
+                        d = col[t];
+                    }
+                    const float mu = fmaf(npx, py[t], bg);
+                    final_pixel<SCMOS, SIG, NB>(d, v, mu, py[t], yd1[t], SIG ? ys1[t] : 0.f, llr, Q);
+                }
+                fisher_column<MODEL, P, NB>(Fm, Q, xp, xd1, xs1, aw);
+                xp = nxp; xd1 = nxd1; xs1 = nxs1;
+            }
+#pragma unroll
+            for (int k = 0; k < P; k++)
+#pragma unroll
+                for (int l = k + 1; l < P; l++) Fm[l][k] = Fm[k][l];
+            if (g < nroi) write_result<P>(a, roi0 + g, valid, th, Fm, llr);
+        }
+    }
+}
+
+// ---- kernel 2: several threads per ROI ------------------------------------------
+//
+// `tpr` lanes (2..32, a power of two) share a ROI: lane r owns a contiguous
+// block of pixel columns and of y-table rows; the group shares the y tables
+// through shared memory and combines its partial sums with warp shuffles.
+// Used for batches too small to fill the GPU with one thread per ROI.
 template <int MODEL, int BOX, bool SCMOS>
 __global__ void __launch_bounds__(256) fit_kernel(const KernelArgs a)
 {
     constexpr int P = ModelInfo<MODEL>::P;
     constexpr bool SIG = ModelInfo<MODEL>::SIG;
+    constexpr bool CROSS = (MODEL == 1 || MODEL == 3);
     constexpr int B2 = BOX * BOX;
     constexpr int NT = ntables<MODEL>();
+    constexpr int PS = SCMOS ? 2 : 1;
+    constexpr int NB = SIG ? 4 : 3;
+    using S = Slots<MODEL>;
 
     extern __shared__ __align__(16) float smem[];
     const int tpr = a.tpr;
     const int R = blockDim.x / tpr;
-    float *sdata = smem;
-    float *svar = sdata + R * B2;
-    int *sok = reinterpret_cast<int *>(svar + (SCMOS ? R * B2 : 0));
+    float *spix = smem;
+    int *sok = reinterpret_cast<int *>(spix + R * B2 * PS);
     float *sytab = reinterpret_cast<float *>(sok + R);
-
     const int64_t roi0 = (int64_t)blockIdx.x * R;
     const int64_t left = a.n - roi0;
     const int nroi = left < R ? (int)left : R;
-
-    // ---- stage the block's ROIs (contiguous in global memory) ----
-    {
-        const float *src = a.data + roi0 * B2;
-        const int cnt = nroi * B2;
-        if ((reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
-            const int c4 = cnt >> 2;
-            const float4 *s4 = reinterpret_cast<const float4 *>(src);
-            float4 *d4 = reinterpret_cast<float4 *>(sdata);
-            for (int e = threadIdx.x; e < c4; e += blockDim.x) d4[e] = __ldg(s4 + e);
-            for (int e = (c4 << 2) + threadIdx.x; e < cnt; e += blockDim.x) sdata[e] = __ldg(src + e);
-        } else {
-            for (int e = threadIdx.x; e < cnt; e += blockDim.x) sdata[e] = __ldg(src + e);
-        }
-        for (int e = cnt + threadIdx.x; e < R * B2; e += blockDim.x) sdata[e] = 0.f;
-        for (int g = threadIdx.x; g < R; g += blockDim.x) {
-            int ok = g < nroi;
-            if (SCMOS && ok) {
-                const int32_t x0 = a.xc[roi0 + g], y0 = a.yc[roi0 + g];
-                ok = x0 >= 1 && y0 >= 1 && x0 + BOX - 1 <= a.nx && y0 + BOX - 1 <= a.ny;
-                if (!ok) atomicAdd(a.bad_corners, 1ull);
-            }
-            sok[g] = ok;
-        }
-    }
-    if (SCMOS) {
-        __syncthreads();
-        // gather the variance tile (and gain/offset for ADU data) of every ROI;
-        // consecutive e walk down a column, i.e. contiguous map addresses.
-        for (int e = threadIdx.x; e < R * B2; e += blockDim.x) {
-            const int g = e / B2, p = e - g * B2;
-            float v = 0.f;
-            if (sok[g]) {
-                const int j = p / BOX, i = p - j * BOX;
-                const int64_t m = (int64_t)(a.yc[roi0 + g] - 1 + i) +
-                                  (int64_t)a.ny * (int64_t)(a.xc[roi0 + g] - 1 + j);
-                v = __ldg(a.var + m);
-                if (a.adu) sdata[e] = __fmul_rn(__fadd_rn(sdata[e], -__ldg(a.offset + m)), __ldg(a.gain + m));
-            }
-            svar[e] = v;
-        }
-    }
-    __syncthreads();
+    stage_block<BOX, SCMOS>(a, spix, sok, R, roi0, nroi);
 
     const int g = threadIdx.x / tpr;  // ROI slot in the block
     const int r = threadIdx.x - g * tpr;
     const int lane = threadIdx.x & 31;
     const int leader = lane & ~(tpr - 1);
-    // Warps without any ROI leave now (no block-wide barrier follows).
+    // this lane's contiguous block of pixel columns (and of y-table rows)
+    const int b0 = (r * BOX) / tpr, b1 = ((r + 1) * BOX) / tpr;
     if (__all_sync(0xffffffffu, g >= nroi)) return;
     const bool valid = g < nroi && sok[g];
-    const float *roi = sdata + g * B2;
-    const float *vroi = svar + g * B2;
+    const float *pix = spix + g * B2 * PS;
     float *ytab = sytab + g * NT * BOX;
 
     float th[P];
 #pragma unroll
     for (int k = 0; k < P; k++) th[k] = 0.f;
-    if (r == 0) initialize<MODEL, BOX>(roi, a.psf, th);
+    if (r == 0) initialize<MODEL, BOX, PS>(pix, a.psf, th);
 #pragma unroll
     for (int k = 0; k < P; k++) th[k] = __shfl_sync(0xffffffffu, th[k], leader);
 
-    float lo[P], hi[P], ms[P];
-#pragma unroll
-    for (int k = 0; k < P; k++) { lo[k] = a.lower[k]; hi[k] = a.upper[k]; ms[k] = a.max_step[k]; }
-
-    // parameter slots
-    constexpr int IX = 0, IY = 1;
-    constexpr int IN = (MODEL == 3) ? 3 : 2;
-    constexpr int IB = (MODEL == 3) ? 4 : 3;
-
-    float yp[BOX], yd1[BOX], yd2[BOX], ys1[SIG ? BOX : 1], ys2[SIG ? BOX : 1];
-
     for (int it = 0; it <= a.iterations; ++it) {
         const bool final_pass = (it == a.iterations);
-        // widths along x and y for this theta
         float sxw, syw;
         AstigWidths aw;
-        if (MODEL == 0) { sxw = syw = a.psf[0]; }
-        else if (MODEL == 1) { sxw = syw = th[4]; }
-        else if (MODEL == 2) { sxw = th[4]; syw = th[5]; }
-        else { astig_widths(th[2], a.psf, aw); sxw = aw.sx; syw = aw.sy; }
-        const float N = th[IN], bg = th[IB];
-        const Axis ax = make_axis(th[IX], sxw, N, a.sqrt2pi, SIG);
-        const Axis ay = make_axis(th[IY], syw, N, a.sqrt2pi, SIG);
+        axis_widths<MODEL>(th, a, sxw, syw, aw);
+        const float N = th[S::IN], bg = th[S::IB];
+        const Axis ax = make_axis(th[S::IX], sxw, N, a.sqrt2pi, SIG);
+        const Axis ay = make_axis(th[S::IY], syw, N, a.sqrt2pi, SIG);
 
-        // ---- y-axis tables (rows), held in registers ----
-        if (tpr == 1) {
-#pragma unroll
-            for (int t = 0; t < BOX; t++) {
-                float s1 = 0.f, s2 = 0.f;
-                axis_entry<SIG, true>(t + 1, ay, yp[t], yd1[t], yd2[t], s1, s2);
-                if (SIG) { ys1[t] = s1; ys2[t] = s2; }
-            }
-        } else {
-            for (int t = r; t < BOX; t += tpr) {
+        // y-axis (row) tables: each lane walks its block of rows; shared memory
+        if (b0 < b1) {
+            EdgeWalk wy = walk_start(b0 + 1, ay);
+            for (int t = b0; t < b1; t++) {
                 float p, d1, d2, s1 = 0.f, s2 = 0.f;
-                axis_entry<SIG, true>(t + 1, ay, p, d1, d2, s1, s2);
-                ytab[t] = p; ytab[BOX + t] = d1; ytab[2 * BOX + t] = d2;
+                walk_entry<SIG, true>(t + 1, ay, wy, p, d1, d2, s1, s2);
+                ytab[t] = p;
+                ytab[BOX + t] = d1;
+                ytab[2 * BOX + t] = d2;
                 if (SIG) { ytab[3 * BOX + t] = s1; ytab[4 * BOX + t] = s2; }
             }
-            __syncwarp();
-#pragma unroll
-            for (int t = 0; t < BOX; t++) {
-                yp[t] = ytab[t]; yd1[t] = ytab[BOX + t]; yd2[t] = ytab[2 * BOX + t];
-                if (SIG) { ys1[t] = ytab[3 * BOX + t]; ys2[t] = ytab[4 * BOX + t]; }
-            }
-            __syncwarp();
         }
+        __syncwarp();
+        float py[BOX];
+#pragma unroll
+        for (int t = 0; t < BOX; t++) py[t] = ytab[t];
+        EdgeWalk wx = walk_start(b0 + 1, ax);
 
         if (!final_pass) {
-            // ---- gradient and diagonal Hessian (src/unified_kernel.jl:314-334) ----
+            float py2[BOX], aG[CROSS ? BOX : 1], C[BOX], D[BOX];
+#pragma unroll
+            for (int t = 0; t < BOX; t++) {
+                py2[t] = py[t] * py[t];
+                if (CROSS) aG[t] = py[t] * ytab[3 * BOX + t];
+                C[t] = 0.f;
+                D[t] = 0.f;
+            }
             float gs[P], hs[P];
 #pragma unroll
             for (int k = 0; k < P; k++) { gs[k] = 0.f; hs[k] = 0.f; }
-            for (int j = r + 1; j <= BOX; j += tpr) {
+            for (int j = b0 + 1; j <= b1; j++) {
                 float xp, xd1, xd2, xs1 = 0.f, xs2 = 0.f;
-                axis_entry<SIG, true>(j, ax, xp, xd1, xd2, xs1, xs2);
-                const float npx = N * xp;
-                const float *col = roi + (j - 1) * BOX;
-                const float *vcol = vroi + (j - 1) * BOX;
+                walk_entry<SIG, true>(j, ax, wx, xp, xd1, xd2, xs1, xs2);
+                const float npx = N * xp, xp2 = xp * xp;
+                const float *col = pix + (j - 1) * BOX * PS;
+                float A = 0.f, B = 0.f, E = 0.f, F = 0.f, Gc = 0.f;
 #pragma unroll
                 for (int t = 0; t < BOX; t++) {
-                    const float py = yp[t];
-                    const float mu = fmaf(npx, py, bg);
-                    const float d = col[t];
-                    float cf, df;
-                    if (!SCMOS) {
-                        if (mu > 0.01f) {
-                            cf = fminf(__fdiv_rn(d, mu) - 1.0f, 1e4f);
-                            df = fminf(__fdiv_rn(d, mu * mu), 1e4f);
-                        } else {
-                            cf = 0.f; df = 0.f;
-                        }
+                    float d, v = 0.f;
+                    if (SCMOS) {
+                        const float2 q = reinterpret_cast<const float2 *>(col)[t];
+                        d = q.x; v = q.y;
                     } else {
-                        const float tv = mu + vcol[t];
-                        cf = __fdiv_rn(d - mu, tv);
-                        df = __fdiv_rn(1.0f, tv);
+                        d = col[t];
                     }
-                    // dudt and diagonal d2udt2 of src/psf_derivatives.jl
-                    const float dux = xd1 * py, d2x = xd2 * py;
-                    const float duy = yd1[t] * xp, d2y = yd2[t] * xp;
-                    const float dun = xp * py;
-                    gs[IX] = fmaf(dux, cf, gs[IX]);
-                    hs[IX] += d2x * cf - dux * dux * df;
-                    gs[IY] = fmaf(duy, cf, gs[IY]);
-                    hs[IY] += d2y * cf - duy * duy * df;
-                    gs[IN] = fmaf(dun, cf, gs[IN]);
-                    hs[IN] -= dun * dun * df;
-                    gs[IB] += cf;
-                    hs[IB] -= df;
-                    if (SIG) {
-                        const float dsx = xs1 * py;
-                        const float ddsx = ax.m2s * dsx - xs2 * py;
-                        const float dsy = ys1[t] * xp;
-                        const float ddsy = ay.m2s * dsy - ys2[t] * xp;
-                        if (MODEL == 1) {
-                            const float du = dsx + dsy, d2 = ddsx + ddsy;
-                            gs[4] = fmaf(du, cf, gs[4]);
-                            hs[4] += d2 * cf - du * du * df;
-                        } else if (MODEL == 2) {
-                            gs[4] = fmaf(dsx, cf, gs[4]);
-                            hs[4] += ddsx * cf - dsx * dsx * df;
-                            gs[5] = fmaf(dsy, cf, gs[5]);
-                            hs[5] += ddsy * cf - dsy * dsy * df;
-                        } else {
-                            const float du = dsx * aw.dsx + dsy * aw.dsy;
-                            const float d2 = ddsx * (aw.dsx * aw.dsx) + dsx * aw.d2sx +
-                                             ddsy * (aw.dsy * aw.dsy) + dsy * aw.d2sy;
-                            gs[2] = fmaf(du, cf, gs[2]);
-                            hs[2] += d2 * cf - du * du * df;
-                        }
-                    }
+                    const float mu = fmaf(npx, py[t], bg);
+                    float cf, df;
+                    likelihood_terms<SCMOS>(d, v, mu, cf, df);
+                    A = fmaf(py[t], cf, A);
+                    B = fmaf(py2[t], df, B);
+                    E += cf;
+                    F += df;
+                    C[t] = fmaf(xp, cf, C[t]);
+                    D[t] = fmaf(xp2, df, D[t]);
+                    if (CROSS) Gc = fmaf(aG[t], df, Gc);
                 }
+                col_terms<MODEL, P>(gs, hs, xp, xd1, xd2, xs1, xs2, A, B, E, F, Gc, ax, aw);
             }
-            // ---- group reduction + scalar Newton step (src/unified_kernel.jl:337-350,
-            //      apply_constraints!, src/constraints.jl:49-53) ----
 #pragma unroll
             for (int k = 0; k < P; k++) {
-                const float G = group_sum(gs[k], tpr);
-                const float H = group_sum(hs[k], tpr);
-                const float delta = fabsf(H) > 1e-10f ? __fdiv_rn(G, H) : 0.f;
-                const float step = jl_clamp(delta, -ms[k], ms[k]);
-                th[k] = jl_clamp(__fadd_rn(th[k], -step), lo[k], hi[k]);
+                gs[k] = group_sum(gs[k], tpr);
+                hs[k] = group_sum(hs[k], tpr);
             }
+#pragma unroll
+            for (int t = 0; t < BOX; t++) {
+                const float Ct = group_sum(C[t], tpr), Dt = group_sum(D[t], tpr);
+                row_terms<MODEL, P>(gs, hs, ytab[BOX + t], ytab[2 * BOX + t],
+                                    SIG ? ytab[3 * BOX + t] : 0.f, SIG ? ytab[4 * BOX + t] : 0.f,
+                                    Ct, Dt, ay, aw);
+            }
+            __syncwarp();  // y-tables are rewritten by the next iteration
+            newton_step<P>(th, gs, hs, a);
         } else {
-            // ---- final pass: LLR + Fisher (src/unified_kernel.jl:354-397) ----
+            float yd1r[BOX], ys1r[SIG ? BOX : 1];
+#pragma unroll
+            for (int t = 0; t < BOX; t++) {
+                yd1r[t] = ytab[BOX + t];
+                if (SIG) ys1r[t] = ytab[3 * BOX + t];
+            }
             float llr = 0.f;
-            double F[P][P];
+            double Fm[P][P];
 #pragma unroll
             for (int k = 0; k < P; k++)
 #pragma unroll
-                for (int l = 0; l < P; l++) F[k][l] = 0.0;
-            for (int j = r + 1; j <= BOX; j += tpr) {
+                for (int l = 0; l < P; l++) Fm[k][l] = 0.0;
+            for (int j = b0 + 1; j <= b1; j++) {
                 float xp, xd1, xd2, xs1 = 0.f, xs2 = 0.f;
-                axis_entry<SIG, false>(j, ax, xp, xd1, xd2, xs1, xs2);
+                walk_entry<SIG, false>(j, ax, wx, xp, xd1, xd2, xs1, xs2);
                 const float npx = N * xp;
-                const float *col = roi + (j - 1) * BOX;
-                const float *vcol = vroi + (j - 1) * BOX;
-                float S[P][P];
+                const float *col = pix + (j - 1) * BOX * PS;
+                float Q[NB][NB];
 #pragma unroll
-                for (int k = 0; k < P; k++)
+                for (int p = 0; p < NB; p++)
 #pragma unroll
-                    for (int l = k; l < P; l++) S[k][l] = 0.f;
+                    for (int q = 0; q < NB; q++) Q[p][q] = 0.f;
 #pragma unroll
                 for (int t = 0; t < BOX; t++) {
-                    const float py = yp[t];
-                    const float mu = fmaf(npx, py, bg);
-                    const float d = col[t];
-                    if (!SCMOS) {
-                        if (mu > 0.f && d > 0.f)
-                            llr += d * logf(mu) - mu - (d * logf(d) - d);
-                        else if (mu > 0.f && d == 0.f)
-                            llr -= mu;
+                    float d, v = 0.f;
+                    if (SCMOS) {
+                        const float2 q = reinterpret_cast<const float2 *>(col)[t];
+                        d = q.x; v = q.y;
                     } else {
-                        const float tv = mu + vcol[t];
-                        if (tv > 0.f) {
-                            const float res = d - mu;
-                            llr += -0.5f * __fdiv_rn(res * res, tv);
-                        }
+                        d = col[t];
                     }
-                    if (mu > 0.f) {
-                        const float w = __fdiv_rn(1.0f, SCMOS ? mu + vcol[t] : mu);
-                        float du[P];
-                        du[IX] = xd1 * py;
-                        du[IY] = yd1[t] * xp;
-                        du[IN] = xp * py;
-                        du[IB] = 1.0f;
-                        if (MODEL == 1) du[4] = xs1 * py + ys1[t] * xp;
-                        if (MODEL == 2) { du[4] = xs1 * py; du[5] = ys1[t] * xp; }
-                        if (MODEL == 3) du[2] = (xs1 * py) * aw.dsx + (ys1[t] * xp) * aw.dsy;
-#pragma unroll
-                        for (int k = 0; k < P; k++) {
-                            const float dkw = du[k] * w;
-#pragma unroll
-                            for (int l = k; l < P; l++) S[k][l] = fmaf(dkw, du[l], S[k][l]);
-                        }
-                    }
+                    const float mu = fmaf(npx, py[t], bg);
+                    final_pixel<SCMOS, SIG, NB>(d, v, mu, py[t], yd1r[t], SIG ? ys1r[t] : 0.f,
+                                                llr, Q);
                 }
-#pragma unroll
-                for (int k = 0; k < P; k++)
-#pragma unroll
-                    for (int l = k; l < P; l++) F[k][l] += (double)S[k][l];
+                fisher_column<MODEL, P, NB>(Fm, Q, xp, xd1, xs1, aw);
             }
             llr = group_sum(llr, tpr);
 #pragma unroll
             for (int k = 0; k < P; k++)
 #pragma unroll
                 for (int l = k; l < P; l++) {
-                    F[k][l] = group_sum(F[k][l], tpr);
-                    F[l][k] = F[k][l];
+                    Fm[k][l] = group_sum(Fm[k][l], tpr);
+                    Fm[l][k] = Fm[k][l];
                 }
-            if (r == 0 && valid) {
-                const int64_t roi = roi0 + g;
-                float cr[P];
-                const uint8_t fl = crlb_from_fisher<P>(F, cr);
-#pragma unroll
-                for (int k = 0; k < P; k++) {
-                    a.params[roi * P + k] = th[k];
-                    a.crlb[roi * P + k] = cr[k];
-                }
-                a.llr[roi] = llr;
-                if (a.flags) a.flags[roi] = fl;
-            } else if (r == 0 && g < nroi) {
-                // corner outside the calibration map: no fit
-                const int64_t roi = roi0 + g;
-                const float qnan = __int_as_float(0x7fc00000);
-#pragma unroll
-                for (int k = 0; k < P; k++) { a.params[roi * P + k] = qnan; a.crlb[roi * P + k] = qnan; }
-                a.llr[roi] = qnan;
-                if (a.flags) a.flags[roi] = 0;
-            }
+            if (r == 0 && g < nroi) write_result<P>(a, roi0 + g, valid, th, Fm, llr);
         }
     }
 }

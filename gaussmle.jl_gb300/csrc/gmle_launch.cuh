@@ -27,23 +27,29 @@ cudaError_t launch_fit_model2(int box, bool scmos, const KernelArgs &a, int rois
 cudaError_t launch_fit_model3(int box, bool scmos, const KernelArgs &a, int rois_per_block,
                               cudaStream_t s);
 
+// Largest block of the one-thread-per-ROI kernel (its __launch_bounds__).
+constexpr int kMaxThreadsR1 = 64;
+
 template <int MODEL, int BOX, bool SCMOS>
 cudaError_t launch_one(const KernelArgs &a, int rois_per_block, cudaStream_t s)
 {
     const int threads = rois_per_block * a.tpr;
     const size_t smem = smem_bytes(MODEL, BOX, SCMOS, a.tpr, rois_per_block);
-    static bool attr_done = false;  // per specialisation; set once per process
-    if (!attr_done) {
-        cudaError_t e = cudaFuncSetAttribute(fit_kernel<MODEL, BOX, SCMOS>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const bool r1 = a.tpr == 1;
+    if (r1 && threads > kMaxThreadsR1) return cudaErrorInvalidConfiguration;
+    void (*kern)(const KernelArgs) = r1 ? fit_kernel_r1<MODEL, BOX, SCMOS>
+                                        : fit_kernel<MODEL, BOX, SCMOS>;
+    static bool attr_done[2] = {false, false};  // per specialisation and kernel
+    if (!attr_done[r1]) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              227 * 1024);
         if (e != cudaSuccess) return e;
-        attr_done = true;
+        attr_done[r1] = true;
     }
     const int64_t blocks = (a.n + rois_per_block - 1) / rois_per_block;
     if (blocks <= 0) return cudaSuccess;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-    fit_kernel<MODEL, BOX, SCMOS><<<(unsigned)blocks, threads, smem, s>>>(a);
+    kern<<<(unsigned)blocks, threads, smem, s>>>(a);
     return cudaGetLastError();
 }
 

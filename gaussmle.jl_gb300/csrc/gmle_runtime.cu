@@ -126,15 +126,17 @@ gmle_status check_desc(gmle_ctx *ctx, const gmle_fit_desc *d)
 // batches), and ROIs per block bounded by shared memory.
 Tuning default_tuning(const gmle_ctx *ctx, int model, int box, bool scmos, int64_t n)
 {
-    const int64_t target_threads = (int64_t)ctx->num_sms * 1024;
+    // Resident ROIs per SM are bounded by shared memory; threads per ROI grow
+    // until about 16 warps per SM are resident and the batch fills the GPU.
+    const size_t per_roi = gmle::smem_bytes(model, box, scmos, 1, 1);
+    const int64_t rois_per_sm = (int64_t)((200 * 1024) / per_roi);
+    const int64_t want_threads_sm = 512;
     int tpr = 1;
-    while (tpr < 8 && n * tpr < target_threads) tpr *= 2;
-    int threads = 128;
-    int rpb = threads / tpr;
-    while (rpb > 1 && gmle::smem_bytes(model, box, scmos, tpr, rpb) > 72 * 1024) {
-        threads /= 2;
-        rpb = threads / tpr;
-    }
+    while (tpr < 4 && (rois_per_sm * tpr < want_threads_sm ||
+                       n * tpr < (int64_t)ctx->num_sms * want_threads_sm))
+        tpr *= 2;
+    int rpb = tpr == 1 ? 32 : 128 / tpr;
+    while (rpb * tpr > 32 && gmle::smem_bytes(model, box, scmos, tpr, rpb) > 100 * 1024) rpb /= 2;
     if (rpb * tpr < 32) rpb = 32 / tpr;
     return {tpr, rpb};
 }
@@ -399,8 +401,7 @@ gmle_status gmle_fit_device(gmle_ctx *ctx, const gmle_fit_desc *desc, const floa
     const Tuning t = pick_tuning(ctx, desc, n);
     KernelArgs a = make_args(ctx, desc, d_data, d_x_corners, d_y_corners, n, d_params, d_crlb,
                              d_llr, d_flags, t.tpr);
-    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->s_fit;
-    CK(launch(ctx, desc, a, t.rois_per_block, s), "fit kernel launch");
+    CK(launch(ctx, desc, a, t.rois_per_block, (cudaStream_t)stream), "fit kernel launch");
     return GMLE_OK;
 }
 
@@ -529,15 +530,20 @@ gmle_status gmle_set_tuning(gmle_ctx *ctx, int32_t model, int32_t box, int32_t c
     if (!ctx) return GMLE_INVALID_ARG;
     std::lock_guard<std::mutex> lk(ctx->mu);
     const int tpr = threads_per_roi;
+    if (tpr == 0 && rois_per_block == 0) {  // forget the entry: size-based default again
+        ctx->tuning.erase({model, box, (int)(camera != GMLE_CAMERA_POISSON)});
+        return GMLE_OK;
+    }
     if (tpr < 1 || tpr > 32 || (tpr & (tpr - 1)))
         return fail(ctx, GMLE_INVALID_ARG, "threads_per_roi must be a power of two in 1..32");
     if (model < 0 || model > 3) return fail(ctx, GMLE_UNSUPPORTED_MODEL, "unknown model");
     if (!gmle::box_supported(box)) return fail(ctx, GMLE_UNSUPPORTED_BOX, "unsupported box");
     const bool scmos = camera != GMLE_CAMERA_POISSON;
     const int threads = tpr * rois_per_block;
-    if (rois_per_block < 1 || threads > 256 || threads % 32)
+    if (rois_per_block < 1 || threads > (tpr == 1 ? gmle::kMaxThreadsR1 : 256) || threads % 32)
         return fail(ctx, GMLE_INVALID_ARG,
-                    "threads_per_roi * rois_per_block must be a multiple of 32, at most 256");
+                    "threads_per_roi * rois_per_block must be a multiple of 32, at most 256 "
+                    "(64 with one thread per ROI)");
     if (gmle::smem_bytes(model, box, scmos, tpr, rois_per_block) > 227 * 1024)
         return fail(ctx, GMLE_INVALID_ARG, "launch shape needs more than 227 KiB shared memory");
     ctx->tuning[{model, box, (int)scmos}] = {tpr, rois_per_block};
@@ -545,5 +551,61 @@ gmle_status gmle_set_tuning(gmle_ctx *ctx, int32_t model, int32_t box, int32_t c
 }
 
 int64_t gmle_kernel_launches(const gmle_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+gmle_status gmle_autotune(gmle_ctx *ctx, const gmle_fit_desc *desc, const float *d_data,
+                          const int32_t *d_x_corners, const int32_t *d_y_corners, int64_t n,
+                          float *d_params, float *d_crlb, float *d_llr, uint8_t *d_flags,
+                          int32_t *threads_per_roi, int32_t *rois_per_block, float *ms_per_fit)
+{
+    if (!ctx) return GMLE_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    gmle_status st = check_desc(ctx, desc);
+    if (st != GMLE_OK) return st;
+    if (n <= 0 || !d_data || !d_params || !d_crlb || !d_llr)
+        return fail(ctx, GMLE_INVALID_ARG, "autotune needs a non-empty device batch");
+    if (desc->camera != GMLE_CAMERA_POISSON && (!d_x_corners || !d_y_corners))
+        return fail(ctx, GMLE_INVALID_ARG, "sCMOS fit needs ROI corners");
+    cudaSetDevice(ctx->device);
+    const bool scmos = desc->camera != GMLE_CAMERA_POISSON;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0), "cudaEventCreate");
+    CK(cudaEventCreate(&e1), "cudaEventCreate");
+    Tuning best{0, 0};
+    float best_ms = 1e30f;
+    for (int tpr = 1; tpr <= 8; tpr *= 2) {
+        for (int threads = 32; threads <= (tpr == 1 ? gmle::kMaxThreadsR1 : 256); threads *= 2) {
+            const int rpb = threads / tpr;
+            if (rpb < 1 || gmle::smem_bytes(desc->model, desc->box, scmos, tpr, rpb) > 227 * 1024)
+                continue;
+            KernelArgs a = make_args(ctx, desc, d_data, d_x_corners, d_y_corners, n, d_params,
+                                     d_crlb, d_llr, d_flags, tpr);
+            cudaError_t e = launch(ctx, desc, a, rpb, ctx->s_fit);  // warm-up
+            if (e == cudaSuccess) e = cudaEventRecord(e0, ctx->s_fit);
+            for (int rep = 0; rep < 2 && e == cudaSuccess; rep++)
+                e = launch(ctx, desc, a, rpb, ctx->s_fit);
+            if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->s_fit);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            float ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            if (e != cudaSuccess) {
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                return cuda_fail(ctx, e, "autotune launch");
+            }
+            ms *= 0.5f;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = {tpr, rpb};
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->tuning[{desc->model, desc->box, (int)scmos}] = best;
+    if (threads_per_roi) *threads_per_roi = best.tpr;
+    if (rois_per_block) *rois_per_block = best.rois_per_block;
+    if (ms_per_fit) *ms_per_fit = best_ms;
+    return GMLE_OK;
+}
 
 }  // extern "C"

@@ -32,7 +32,7 @@ CAMERA_SCMOS_ADU = 2
 EXPORTED = [
     "gmle_abi_version", "gmle_create", "gmle_destroy", "gmle_last_error",
     "gmle_set_calibration", "gmle_fit", "gmle_fit_device", "gmle_fit_device_errors",
-    "gmle_get_tuning", "gmle_set_tuning", "gmle_kernel_launches",
+    "gmle_get_tuning", "gmle_set_tuning", "gmle_autotune", "gmle_kernel_launches",
 ]
 
 
@@ -86,6 +86,8 @@ def load(path: str | Path | None = None) -> C.CDLL:
             "gmle_fit_device_errors": ([vp, C.POINTER(i64)], C.c_int),
             "gmle_get_tuning": ([vp, i32, i32, i32, C.POINTER(i32), C.POINTER(i32)], C.c_int),
             "gmle_set_tuning": ([vp, i32, i32, i32, i32, i32], C.c_int),
+            "gmle_autotune": ([vp, C.POINTER(FitDesc), vp, vp, vp, i64, vp, vp, vp, vp,
+                               C.POINTER(i32), C.POINTER(i32), C.POINTER(C.c_float)], C.c_int),
             "gmle_kernel_launches": ([vp], i64),
         }
         for name, (args, res) in sigs.items():

@@ -135,7 +135,8 @@ gmle_status gmle_fit(gmle_ctx *ctx, const gmle_fit_desc *desc, const float *data
 /*
  * Asynchronous fit of n ROIs already resident in DEVICE memory (for callers
  * that hold device arrays, e.g. a CuArray): enqueues the fit kernel on
- * `stream` (a cudaStream_t; NULL = the context's stream) and returns.  All
+ * `stream` (a cudaStream_t, used as given: NULL is the legacy default
+ * stream, as everywhere in CUDA) and returns.  All
  * pointers are device pointers; flags may be NULL.  Corners outside the
  * calibration map are reported through gmle_fit_device_errors().
  */
@@ -150,12 +151,27 @@ gmle_status gmle_fit_device_errors(gmle_ctx *ctx, int64_t *count);
 
 /*
  * Kernel launch shape used for a (model, box, camera): threads per ROI and
- * ROIs per block, as picked by the autotuner (or set by gmle_set_tuning).
+ * ROIs per block, as picked by the autotuner (or set by gmle_set_tuning;
+ * setting (0, 0) forgets the entry and restores the size-based default).
+ * One thread per ROI allows at most 64 ROIs per block.
  */
 gmle_status gmle_get_tuning(gmle_ctx *ctx, int32_t model, int32_t box, int32_t camera,
                             int32_t *threads_per_roi, int32_t *rois_per_block);
 gmle_status gmle_set_tuning(gmle_ctx *ctx, int32_t model, int32_t box, int32_t camera,
                             int32_t threads_per_roi, int32_t rois_per_block);
+
+/*
+ * Autotuner: times every candidate launch shape (threads per ROI 1, 2, 4, 8;
+ * 32..256 threads per block, within 227 KiB of shared memory) of the fit
+ * kernel for `desc` on a device-resident batch, keeps the fastest for
+ * (model, box, camera family) in the context and returns it with its time
+ * per launch.  The output buffers are overwritten.  No reference counterpart:
+ * KernelAbstractions picks the reference's workgroup size.
+ */
+gmle_status gmle_autotune(gmle_ctx *ctx, const gmle_fit_desc *desc, const float *d_data,
+                          const int32_t *d_x_corners, const int32_t *d_y_corners, int64_t n,
+                          float *d_params, float *d_crlb, float *d_llr, uint8_t *d_flags,
+                          int32_t *threads_per_roi, int32_t *rois_per_block, float *ms_per_fit);
 
 /* Number of fit-kernel launches this context has issued (for accounting). */
 int64_t gmle_kernel_launches(const gmle_ctx *ctx);

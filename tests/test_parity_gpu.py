@@ -81,3 +81,24 @@ def test_device_entry_matches_host_entry(ctx):
     assert np.array_equal(params.cpu().numpy(), hp)
     assert np.array_equal(crlb.cpu().numpy(), hc)
     assert np.array_equal(flags.cpu().numpy(), hf)
+
+
+SHAPE_CASES = [c for c in CASES if c[0] in ("xynb-11-poisson", "xynbs-13-scmos-adu",
+                                           "xynbsxsy-13-scmos-adu", "astig-15-poisson")]
+
+
+@pytest.mark.parametrize("tpr,rpb", [(1, 32), (1, 64), (2, 32), (4, 32), (8, 16)])
+@pytest.mark.parametrize("case", SHAPE_CASES, ids=[c[0] for c in SHAPE_CASES])
+def test_parity_every_launch_shape(ctx, case, tpr, rpb):
+    """Both kernels (one thread per ROI, and lane groups of 2..8) meet the bar."""
+    name, model, box, camera, n = case
+    w = make_case(name, model, box, camera, min(n, 1500))
+    ctx.check(ctx.lib.gmle_set_tuning(ctx.handle, model, box, camera, tpr, rpb))
+    try:
+        params, crlb, llr, flags = run_gpu(ctx, w)
+    finally:
+        # (0, 0) removes the entry: back to the size-based default
+        ctx.check(ctx.lib.gmle_set_tuning(ctx.handle, model, box, camera, 0, 0))
+    ref = O.fit(oracle_desc(O, w), w.data, w.x_corners, w.y_corners, w.maps, "f32")
+    ok, st = compare(model, params, crlb, flags, ref)
+    assert st["pass_frac"] >= MIN_PASS.get(w.name, DEFAULT_MIN_PASS), (tpr, rpb, st)
