@@ -418,64 +418,96 @@ __device__ uint8_t crlb_from_fisher(double (&F)[P][P], float *crlb)
 // ---- shared pieces of the two kernels ----------------------------------------
 
 // Shared memory, as arrays over the R ROI slots of a block: pixels (float, or
-// float2 (data in e-, read-noise variance) for sCMOS), one ok flag per slot,
-// and, when several lanes share a ROI (tpr > 1), NT * BOX y-axis table entries.
+// float2 (data in e-, read-noise variance) for sCMOS), for sCMOS the map
+// offset of each ROI's first pixel (int64), one ok flag per slot, and, when
+// several lanes share a ROI (tpr > 1), NT * BOX y-axis table entries.
 inline size_t smem_bytes(int model, int box, bool scmos, int tpr, int rois)
 {
     const int nt = model == 0 ? 3 : 5;
     return (size_t)rois * (sizeof(float) * ((size_t)box * box * (scmos ? 2 : 1) +
                                             (tpr > 1 ? (size_t)nt * box : 0)) +
-                           sizeof(int));
+                           (scmos ? sizeof(long long) : 0) + sizeof(int));
 }
 
-// Stage the block's R ROIs (contiguous in global memory) into shared memory;
-// for sCMOS gather the variance tile from the resident map and apply the
-// ADU -> e- conversion of src/camera_models.jl:110-113 on the way.
+// Asynchronous global -> shared copies (cp.async, sm_80+ PTX); src_bytes = 0
+// fills the destination with zeros without reading the source.
+__device__ __forceinline__ void cp_async4(void *dst, const void *src, unsigned src_bytes)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(src),
+                 "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *dst, const void *src)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+// Stage the block's R ROIs (contiguous in global memory) into shared memory.
+// All pixel (and variance-tile) copies of a thread are issued as cp.async
+// before any is waited for; for sCMOS the variance tile is gathered from the
+// resident map and ADU data are converted, (ADU - offset) * gain
+// (src/camera_models.jl:110-113), with the gain/offset loads batched.
 template <int BOX, bool SCMOS>
 __device__ __forceinline__ void stage_block(const KernelArgs &a, float *spix, int *sok, int R,
                                             int64_t roi0, int nroi)
 {
     constexpr int B2 = BOX * BOX;
+    long long *sbase = reinterpret_cast<long long *>(spix + R * B2 * (SCMOS ? 2 : 1));
     for (int g = threadIdx.x; g < R; g += blockDim.x) {
         int ok = g < nroi;
+        long long base = 0;
         if (SCMOS && ok) {
             const int32_t x0 = a.xc[roi0 + g], y0 = a.yc[roi0 + g];
             ok = x0 >= 1 && y0 >= 1 && x0 + BOX - 1 <= a.nx && y0 + BOX - 1 <= a.ny;
             if (!ok) atomicAdd(a.bad_corners, 1ull);
+            base = (long long)(y0 - 1) + (long long)a.ny * (long long)(x0 - 1);
         }
         sok[g] = ok;
+        if (SCMOS) sbase[g] = base;
     }
     const float *src = a.data + roi0 * B2;
     const int cnt = nroi * B2;
     if (!SCMOS) {
         if ((reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
             const int c4 = cnt >> 2;
-            const float4 *s4 = reinterpret_cast<const float4 *>(src);
-            float4 *d4 = reinterpret_cast<float4 *>(spix);
-            for (int e = threadIdx.x; e < c4; e += blockDim.x) d4[e] = __ldg(s4 + e);
-            for (int e = (c4 << 2) + threadIdx.x; e < cnt; e += blockDim.x) spix[e] = __ldg(src + e);
+            for (int e = threadIdx.x; e < c4; e += blockDim.x)
+                cp_async16(spix + 4 * e, src + 4 * e);
+            for (int e = (c4 << 2) + threadIdx.x; e < cnt; e += blockDim.x)
+                cp_async4(spix + e, src + e, 4);
         } else {
-            for (int e = threadIdx.x; e < cnt; e += blockDim.x) spix[e] = __ldg(src + e);
+            for (int e = threadIdx.x; e < cnt; e += blockDim.x) cp_async4(spix + e, src + e, 4);
         }
         for (int e = cnt + threadIdx.x; e < R * B2; e += blockDim.x) spix[e] = 0.f;
+        cp_async_wait_all();
     } else {
-        __syncthreads();  // sok
+        __syncthreads();  // sok, sbase
         // consecutive e walk down a column: contiguous map addresses
-        float2 *s2 = reinterpret_cast<float2 *>(spix);
         for (int e = threadIdx.x; e < R * B2; e += blockDim.x) {
             const int g = e / B2;
-            float2 v = make_float2(0.f, 0.f);
-            if (e < cnt) {
-                v.x = __ldg(src + e);
+            const int p = e - g * B2, j = p / BOX, i = p - j * BOX;
+            const bool in = e < cnt;
+            const bool okg = in && sok[g];
+            const long long m = sbase[g] + i + (long long)a.ny * j;
+            cp_async4(spix + 2 * e, in ? src + e : a.data, in ? 4u : 0u);
+            cp_async4(spix + 2 * e + 1, okg ? a.var + m : a.var, okg ? 4u : 0u);
+        }
+        cp_async_wait_all();
+        if (a.adu) {
+#pragma unroll 4
+            for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
+                const int g = e / B2;
                 if (sok[g]) {
                     const int p = e - g * B2, j = p / BOX, i = p - j * BOX;
-                    const int64_t m = (int64_t)(a.yc[roi0 + g] - 1 + i) +
-                                      (int64_t)a.ny * (int64_t)(a.xc[roi0 + g] - 1 + j);
-                    if (a.adu) v.x = __fmul_rn(__fadd_rn(v.x, -__ldg(a.offset + m)), __ldg(a.gain + m));
-                    v.y = __ldg(a.var + m);
+                    const long long m = sbase[g] + i + (long long)a.ny * j;
+                    const float off = __ldg(a.offset + m), gn = __ldg(a.gain + m);
+                    spix[2 * e] = __fmul_rn(__fadd_rn(spix[2 * e], -off), gn);
                 }
             }
-            s2[e] = v;
         }
     }
     __syncthreads();
@@ -701,8 +733,13 @@ __device__ __forceinline__ void axis_widths(const float *th, const KernelArgs &a
 // next column's erf/exp evaluations are issued before the current column's
 // pixel work so that their latency overlaps it.  Occupancy is bounded by
 // shared memory (the staged pixels), so registers are not the constraint.
+//
+// fit_rois_r1 fits ROIs [roi0, roi0 + nroi) of `a` (nroi <= blockDim.x) with
+// the block's threads, staging them in `smem`; the plain kernel calls it once
+// per block, the persistent mixed-batch kernel once per work tile.
 template <int MODEL, int BOX, bool SCMOS>
-__global__ void __launch_bounds__(64) fit_kernel_r1(const KernelArgs a)
+__device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, int nroi,
+                                            float *smem)
 {
     constexpr int P = ModelInfo<MODEL>::P;
     constexpr bool SIG = ModelInfo<MODEL>::SIG;
@@ -712,13 +749,9 @@ __global__ void __launch_bounds__(64) fit_kernel_r1(const KernelArgs a)
     constexpr int NB = SIG ? 4 : 3;
     using S = Slots<MODEL>;
 
-    extern __shared__ __align__(16) float smem[];
     const int R = blockDim.x;
     float *spix = smem;
-    int *sok = reinterpret_cast<int *>(spix + R * B2 * PS);
-    const int64_t roi0 = (int64_t)blockIdx.x * R;
-    const int64_t left = a.n - roi0;
-    const int nroi = left < R ? (int)left : R;
+    int *sok = reinterpret_cast<int *>(spix + R * B2 * PS + (SCMOS ? 2 * R : 0));
     stage_block<BOX, SCMOS>(a, spix, sok, R, roi0, nroi);
 
     const int g = threadIdx.x;
@@ -841,6 +874,16 @@ __global__ void __launch_bounds__(64) fit_kernel_r1(const KernelArgs a)
     }
 }
 
+template <int MODEL, int BOX, bool SCMOS>
+__global__ void __launch_bounds__(64) fit_kernel_r1(const KernelArgs a)
+{
+    extern __shared__ __align__(16) float smem[];
+    const int R = blockDim.x;
+    const int64_t roi0 = (int64_t)blockIdx.x * R;
+    const int64_t left = a.n - roi0;
+    fit_rois_r1<MODEL, BOX, SCMOS>(a, roi0, left < R ? (int)left : R, smem);
+}
+
 // ---- kernel 2: several threads per ROI ------------------------------------------
 //
 // `tpr` lanes (2..32, a power of two) share a ROI: lane r owns a contiguous
@@ -863,7 +906,7 @@ __global__ void __launch_bounds__(256) fit_kernel(const KernelArgs a)
     const int tpr = a.tpr;
     const int R = blockDim.x / tpr;
     float *spix = smem;
-    int *sok = reinterpret_cast<int *>(spix + R * B2 * PS);
+    int *sok = reinterpret_cast<int *>(spix + R * B2 * PS + (SCMOS ? 2 * R : 0));
     float *sytab = reinterpret_cast<float *>(sok + R);
     const int64_t roi0 = (int64_t)blockIdx.x * R;
     const int64_t left = a.n - roi0;

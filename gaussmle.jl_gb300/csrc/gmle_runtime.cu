@@ -19,61 +19,16 @@
 #include <mutex>
 #include <string>
 #include <tuple>
+#include <vector>
 
-#include "../../include/gaussmle_gb300.h"
-#include "gmle_launch.cuh"
-
-namespace {
+#include "gmle_internal.h"
 
 using gmle::KernelArgs;
+using namespace gmle_rt;
+
+namespace gmle_rt {
 
 int nparams(int model) { return model == 0 ? 4 : (model == 2 ? 6 : 5); }
-
-struct Tuning {
-    int tpr;
-    int rois_per_block;
-};
-
-// One pipeline slot of device buffers for the host-buffer path.
-struct Slot {
-    float *data = nullptr;
-    int32_t *xc = nullptr, *yc = nullptr;
-    float *params = nullptr, *crlb = nullptr, *llr = nullptr;
-    uint8_t *flags = nullptr;
-    int64_t cap_rois = 0;   // ROIs the buffers hold
-    int64_t cap_b2 = 0;     // box^2 the data buffer was sized for
-    // pinned staging for pageable caller memory
-    float *h_data = nullptr;
-    float *h_params = nullptr, *h_crlb = nullptr, *h_llr = nullptr;
-    uint8_t *h_flags = nullptr;
-    int64_t h_cap_rois = 0, h_cap_b2 = 0;
-    cudaEvent_t h2d_done = nullptr, fit_done = nullptr, d2h_done = nullptr;
-    // pending copy of pinned outputs to pageable caller memory
-    bool pending = false;
-    float *dst_params = nullptr, *dst_crlb = nullptr, *dst_llr = nullptr;
-    uint8_t *dst_flags = nullptr;
-    int64_t pend_rois = 0;
-    int pend_p = 0;
-};
-
-}  // namespace
-
-struct gmle_ctx {
-    int device = 0;
-    int num_sms = 0;
-    cudaStream_t s_fit = nullptr, s_h2d = nullptr, s_d2h = nullptr;
-    std::string err;
-    std::mutex mu;
-    // resident calibration maps, (ny, nx) column-major
-    float *d_var = nullptr, *d_gain = nullptr, *d_offset = nullptr;
-    int32_t ny = 0, nx = 0;
-    unsigned long long *d_bad = nullptr;
-    int64_t launches = 0;
-    std::map<std::tuple<int, int, int>, Tuning> tuning;
-    Slot slots[2];
-};
-
-namespace {
 
 gmle_status fail(gmle_ctx *ctx, gmle_status st, const char *fmt, ...)
 {
@@ -93,11 +48,7 @@ gmle_status cuda_fail(gmle_ctx *ctx, cudaError_t e, const char *what)
     return fail(ctx, GMLE_CUDA_ERROR, "%s: %s", what, cudaGetErrorString(e));
 }
 
-#define CK(call, what)                                      \
-    do {                                                    \
-        cudaError_t e_ = (call);                            \
-        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
-    } while (0)
+#define CK(call, what) GMLE_CK(call, what)
 
 gmle_status check_desc(gmle_ctx *ctx, const gmle_fit_desc *d)
 {
@@ -121,6 +72,10 @@ gmle_status check_desc(gmle_ctx *ctx, const gmle_fit_desc *d)
         return fail(ctx, GMLE_INVALID_ARG, "astigmatic sigma0 must be > 0 and d != 0");
     return GMLE_OK;
 }
+
+}  // namespace gmle_rt
+
+namespace {
 
 // Launch shape: enough threads to fill the GPU (threads per ROI grows for small
 // batches), and ROIs per block bounded by shared memory.
@@ -335,7 +290,9 @@ void gmle_destroy(gmle_ctx *ctx)
     if (ctx->s_fit) cudaStreamSynchronize(ctx->s_fit);
     if (ctx->s_h2d) cudaStreamSynchronize(ctx->s_h2d);
     if (ctx->s_d2h) cudaStreamSynchronize(ctx->s_d2h);
+    server_destroy(ctx);
     for (Slot &s : ctx->slots) free_slot(s);
+    for (MixedBufs &b : ctx->mixed) free_mixed(b);
     cudaFree(ctx->d_var);
     cudaFree(ctx->d_gain);
     cudaFree(ctx->d_offset);
@@ -609,3 +566,184 @@ gmle_status gmle_autotune(gmle_ctx *ctx, const gmle_fit_desc *desc, const float 
 }
 
 }  // extern "C"
+
+// ---- mixed batches: one persistent work-stealing launch per camera family ------
+
+namespace gmle_rt {
+
+namespace {
+
+double group_cost(const gmle_fit_desc &d)
+{
+    return (double)d.box * d.box * (nparams(d.model) + (d.model == 3 ? 3 : 0));
+}
+
+}  // namespace
+
+gmle_status ensure_mixed(gmle_ctx *ctx, MixedBufs &b, int ngroups)
+{
+    if (!b.reuse) {
+        CK(cudaEventCreateWithFlags(&b.reuse, cudaEventDisableTiming), "cudaEventCreate");
+        CK(cudaMallocHost(&b.h_header, 2 * sizeof(int64_t)), "cudaMallocHost(header)");
+        CK(cudaMalloc(&b.d_counter, sizeof(unsigned long long)), "cudaMalloc(counter)");
+    }
+    if (b.cap < ngroups) {
+        CK(cudaEventSynchronize(b.reuse), "cudaEventSynchronize");
+        cudaFreeHost(b.h_groups);
+        b.h_groups = nullptr;
+        b.cap = 0;
+        const int cap = std::max(64, ngroups);
+        CK(cudaMallocHost(&b.h_groups, sizeof(gmle::GroupDesc) * cap), "cudaMallocHost(groups)");
+        b.cap = cap;
+    }
+    return GMLE_OK;
+}
+
+gmle_status free_mixed(MixedBufs &b)
+{
+    if (b.reuse) cudaEventSynchronize(b.reuse);
+    cudaFreeHost(b.h_groups);
+    cudaFreeHost(b.h_header);
+    cudaFree(b.d_counter);
+    if (b.reuse) cudaEventDestroy(b.reuse);
+    b = MixedBufs();
+    return GMLE_OK;
+}
+
+size_t mixed_smem(const gmle_group *groups, int32_t ngroups, bool scmos)
+{
+    size_t m = 0;
+    for (int k = 0; k < ngroups; k++) {
+        const gmle_fit_desc &d = groups[k].desc;
+        if ((d.camera != GMLE_CAMERA_POISSON) != scmos || groups[k].n <= 0) continue;
+        m = std::max(m, gmle::smem_bytes(d.model, d.box, scmos, 1, gmle::kMixedTile));
+    }
+    return m;
+}
+
+gmle_status validate_groups(gmle_ctx *ctx, const gmle_group *groups, int32_t ngroups)
+{
+    for (int k = 0; k < ngroups; k++) {
+        const gmle_group &G = groups[k];
+        gmle_status st = check_desc(ctx, &G.desc);
+        if (st != GMLE_OK) return st;
+        if (!gmle::mixed_box(G.desc.box))
+            return fail(ctx, GMLE_UNSUPPORTED_BOX, "group %d: box %d not in the mixed kernel", k,
+                        G.desc.box);
+        if (G.n < 0) return fail(ctx, GMLE_INVALID_ARG, "group %d: n < 0", k);
+        if (G.n > 0 && (!G.data || !G.params || !G.crlb || !G.llr))
+            return fail(ctx, GMLE_INVALID_ARG, "group %d: data and output pointers are required", k);
+        if (G.n > 0 && G.desc.camera != GMLE_CAMERA_POISSON && (!G.x_corners || !G.y_corners))
+            return fail(ctx, GMLE_INVALID_ARG, "group %d: sCMOS fit needs ROI corners", k);
+    }
+    return GMLE_OK;
+}
+
+int64_t build_mixed_table(gmle_ctx *ctx, const gmle_group *groups, int32_t ngroups, bool scmos,
+                          MixedBufs &b, gmle_status *st)
+{
+    *st = GMLE_OK;
+    std::vector<int> idx;
+    for (int k = 0; k < ngroups; k++)
+        if ((groups[k].desc.camera != GMLE_CAMERA_POISSON) == scmos && groups[k].n > 0)
+            idx.push_back(k);
+    if (idx.empty()) return 0;
+    // most expensive ROIs first: the heavy tiles start early, the tail is short
+    std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) {
+        return group_cost(groups[x].desc) > group_cost(groups[y].desc);
+    });
+    *st = ensure_mixed(ctx, b, (int)idx.size());
+    if (*st != GMLE_OK) return 0;
+    if (cudaEventSynchronize(b.reuse) != cudaSuccess) {  // the pinned table is free
+        *st = cuda_fail(ctx, cudaGetLastError(), "cudaEventSynchronize");
+        return 0;
+    }
+    int64_t tiles = 0;
+    for (size_t q = 0; q < idx.size(); q++) {
+        const gmle_group &G = groups[idx[q]];
+        gmle::GroupDesc &D = b.h_groups[q];
+        D.data = G.data;
+        D.xc = G.x_corners;
+        D.yc = G.y_corners;
+        D.n = G.n;
+        D.params = G.params;
+        D.crlb = G.crlb;
+        D.llr = G.llr;
+        D.flags = G.flags;
+        D.model = G.desc.model;
+        D.box = G.desc.box;
+        D.iterations = G.desc.iterations;
+        D.adu = G.desc.camera == GMLE_CAMERA_SCMOS_ADU;
+        std::memcpy(D.psf, G.desc.psf, sizeof D.psf);
+        std::memcpy(D.lower, G.desc.lower, sizeof D.lower);
+        std::memcpy(D.upper, G.desc.upper, sizeof D.upper);
+        std::memcpy(D.max_step, G.desc.max_step, sizeof D.max_step);
+        D.tile0 = tiles;
+        tiles += (G.n + gmle::kMixedTile - 1) / gmle::kMixedTile;
+    }
+    b.h_header[0] = (int64_t)idx.size();
+    b.h_header[1] = tiles;
+    return tiles;
+}
+
+int mixed_grid(gmle_ctx *ctx, bool scmos, size_t smem)
+{
+    return ctx->num_sms * std::max(1, gmle::mixed_blocks_per_sm(scmos, smem));
+}
+
+gmle_status enqueue_mixed(gmle_ctx *ctx, bool scmos, MixedBufs &b, size_t smem, int grid,
+                          cudaStream_t s)
+{
+    // The kernel reads the group table straight from pinned host memory (a
+    // few hundred bytes per tile of 32 ROIs), so a launch needs no table copy
+    // and a captured graph stays valid for any table contents.
+    CK(cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned long long), s), "reset tile counter");
+    gmle::MixedArgs m;
+    m.groups = b.h_groups;
+    m.header = b.h_header;
+    m.tile_counter = b.d_counter;
+    m.var = ctx->d_var;
+    m.gain = ctx->d_gain;
+    m.offset = ctx->d_offset;
+    m.ny = ctx->ny;
+    m.nx = ctx->nx;
+    m.rois_per_tile = gmle::kMixedTile;
+    m.sqrt2pi = sqrtf(2.0f * (float)3.14159265358979323846);
+    m.bad_corners = ctx->d_bad;
+    CK(gmle::launch_mixed(scmos, m, smem, grid, s), "mixed kernel launch");
+    return GMLE_OK;
+}
+
+gmle_status run_mixed(gmle_ctx *ctx, const gmle_group *groups, int32_t ngroups, cudaStream_t s,
+                      MixedBufs *bufs)
+{
+    gmle_status st = validate_groups(ctx, groups, ngroups);
+    if (st != GMLE_OK) return st;
+    for (int fam = 0; fam < 2; fam++) {
+        const bool scmos = fam == 1;
+        MixedBufs &b = bufs[fam];
+        const int64_t tiles = build_mixed_table(ctx, groups, ngroups, scmos, b, &st);
+        if (st != GMLE_OK) return st;
+        if (tiles == 0) continue;
+        const size_t smem = mixed_smem(groups, ngroups, scmos);
+        const int grid = (int)std::min<int64_t>(mixed_grid(ctx, scmos, smem), tiles);
+        ctx->launches++;
+        st = enqueue_mixed(ctx, scmos, b, smem, grid, s);
+        if (st != GMLE_OK) return st;
+        CK(cudaEventRecord(b.reuse, s), "cudaEventRecord");  // the table may be rewritten after this
+    }
+    return GMLE_OK;
+}
+
+}  // namespace gmle_rt
+
+extern "C" gmle_status gmle_fit_mixed_device(gmle_ctx *ctx, const gmle_group *groups,
+                                             int32_t ngroups, void *stream)
+{
+    if (!ctx) return GMLE_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (ngroups < 0 || (ngroups > 0 && !groups))
+        return fail(ctx, GMLE_INVALID_ARG, "groups array is required");
+    cudaSetDevice(ctx->device);
+    return run_mixed(ctx, groups, ngroups, (cudaStream_t)stream, ctx->mixed);
+}

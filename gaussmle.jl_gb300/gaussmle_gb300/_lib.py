@@ -33,6 +33,8 @@ EXPORTED = [
     "gmle_abi_version", "gmle_create", "gmle_destroy", "gmle_last_error",
     "gmle_set_calibration", "gmle_fit", "gmle_fit_device", "gmle_fit_device_errors",
     "gmle_get_tuning", "gmle_set_tuning", "gmle_autotune", "gmle_kernel_launches",
+    "gmle_fit_mixed_device", "gmle_server_start", "gmle_server_stop", "gmle_submit",
+    "gmle_poll", "gmle_wait", "gmle_server_stats_get",
 ]
 
 
@@ -44,6 +46,36 @@ class FitDesc(C.Structure):
         ("camera", C.c_int32), ("psf", C.c_float * 8), ("lower", C.c_float * 6),
         ("upper", C.c_float * 6), ("max_step", C.c_float * 6),
     ]
+
+
+class Group(C.Structure):
+    """gmle_group: one homogeneous group of a mixed batch / one serving request."""
+    _fields_ = [
+        ("desc", FitDesc), ("data", C.c_void_p), ("x_corners", C.c_void_p),
+        ("y_corners", C.c_void_p), ("n", C.c_int64), ("params", C.c_void_p),
+        ("crlb", C.c_void_p), ("llr", C.c_void_p), ("flags", C.c_void_p),
+    ]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [
+        ("hbm_budget_bytes", C.c_int64), ("max_inflight_steps", C.c_int32),
+        ("max_step_rois", C.c_int64), ("max_pending", C.c_int32), ("use_graphs", C.c_int32),
+    ]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [
+        ("submitted", C.c_int64), ("completed", C.c_int64), ("rejected", C.c_int64),
+        ("failed", C.c_int64), ("rois_completed", C.c_int64), ("steps", C.c_int64),
+        ("p50_latency_ms", C.c_double), ("p99_latency_ms", C.c_double),
+        ("mean_latency_ms", C.c_double), ("max_latency_ms", C.c_double),
+        ("fits_per_s", C.c_double), ("hbm_budget_bytes", C.c_int64),
+        ("hbm_in_use_bytes", C.c_int64), ("hbm_peak_bytes", C.c_int64),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class GaussMLEError(RuntimeError):
@@ -89,6 +121,13 @@ def load(path: str | Path | None = None) -> C.CDLL:
             "gmle_autotune": ([vp, C.POINTER(FitDesc), vp, vp, vp, i64, vp, vp, vp, vp,
                                C.POINTER(i32), C.POINTER(i32), C.POINTER(C.c_float)], C.c_int),
             "gmle_kernel_launches": ([vp], i64),
+            "gmle_fit_mixed_device": ([vp, C.POINTER(Group), i32, vp], C.c_int),
+            "gmle_server_start": ([vp, C.POINTER(ServerConfig)], C.c_int),
+            "gmle_server_stop": ([vp], C.c_int),
+            "gmle_submit": ([vp, C.POINTER(Group), C.POINTER(C.c_uint64)], C.c_int),
+            "gmle_poll": ([vp, C.c_uint64], C.c_int),
+            "gmle_wait": ([vp, C.c_uint64, i64], C.c_int),
+            "gmle_server_stats_get": ([vp, C.POINTER(ServerStats), i32], C.c_int),
         }
         for name, (args, res) in sigs.items():
             f = getattr(lib, name)

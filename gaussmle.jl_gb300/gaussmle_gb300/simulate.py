@@ -281,3 +281,61 @@ def config1_device(n: int = 1_000_000, seed: int = 1001, sensor: int = 2048, dev
     data = (e / gg + oo).float().contiguous().view(-1)
     return {"data": data, "xc": xc, "yc": yc, "var": var, "gain": gain, "offset": off,
             "truth": truth, "box": box, "n": n, "ny": sensor, "nx": sensor}
+
+
+def device_workload(model: int, box: int, camera: int, n: int, seed: int = 2024,
+                    sensor: int = 2048, device="cuda"):
+    """A homogeneous on-device batch of any (model, box, camera) with the
+    distributions of the mixed workload (x, y within +-1.5 px of the centre,
+    N U(500, 5000), bg U(1, 20); sigma U(1.0, 1.8); sigma_x, sigma_y U(1, 2);
+    astigmatic z U(-400, 400) with the (1.3, 1.3, 0.05, 0.05, 0.3, 0.3, 50,
+    100) calibration).  Same return layout as config1_device()."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    f64 = dict(dtype=torch.float64, device=device)
+    c = (box + 1) / 2.0
+    u = lambda lo, hi: lo + (hi - lo) * torch.rand(n, generator=g, **f64)
+    x, y, N, bg = u(c - 1.5, c + 1.5), u(c - 1.5, c + 1.5), u(500, 5000), u(1, 20)
+    if model == MODEL_XYNB:
+        psf = GaussianXYNB(1.3)
+        sx = sy = torch.full((n,), 1.3, **f64)
+        truth = torch.stack([x, y, N, bg], 1)
+    elif model == MODEL_XYNBS:
+        psf = GaussianXYNBS()
+        sx = sy = u(1.0, 1.8)
+        truth = torch.stack([x, y, N, bg, sx], 1)
+    elif model == MODEL_XYNBSXSY:
+        psf = GaussianXYNBSXSY()
+        sx, sy = u(1.0, 2.0), u(1.0, 2.0)
+        truth = torch.stack([x, y, N, bg, sx, sy], 1)
+    else:
+        psf = AstigmaticXYZNB(1.3, 1.3, 0.05, 0.05, 0.3, 0.3, 50.0, 100.0)
+        z = u(-400, 400)
+        zx, zy = (z - psf.gamma) / psf.d, (z + psf.gamma) / psf.d
+        sx = psf.sx0 * torch.sqrt(1 + zx ** 2 + psf.Ax * zx ** 3 + psf.Bx * zx ** 4)
+        sy = psf.sy0 * torch.sqrt(1 + zy ** 2 + psf.Ay * zy ** 3 + psf.By * zy ** 4)
+        truth = torch.stack([x, y, z, N, bg], 1)
+    px = _psf_1d_t(torch, x, sx, box)
+    py = _psf_1d_t(torch, y, sy, box)
+    mu = bg[:, None, None] + N[:, None, None] * px[:, :, None] * py[:, None, :]
+    e = torch.poisson(mu, generator=g)
+    out = {"truth": truth.float(), "box": box, "n": n, "psf": psf, "model": model,
+           "camera": camera, "ny": 0, "nx": 0, "xc": None, "yc": None}
+    if camera:
+        var = torch.exp(np.log(2.0) + 0.5 * torch.randn((sensor, sensor), generator=g, **f64)).float()
+        gain = (0.4 + 0.2 * torch.rand((sensor, sensor), generator=g, **f64)).float()
+        off = torch.full((sensor, sensor), 100.0, dtype=torch.float32, device=device)
+        xc = torch.randint(1, sensor - box + 2, (n,), generator=g, device=device, dtype=torch.int32)
+        yc = torch.randint(1, sensor - box + 2, (n,), generator=g, device=device, dtype=torch.int32)
+        jj = torch.arange(box, device=device)[None, :, None]
+        ii = torch.arange(box, device=device)[None, None, :]
+        cols = (xc.long()[:, None, None] - 1) + jj
+        rows = (yc.long()[:, None, None] - 1) + ii
+        v = var[cols, rows].double()
+        e = e + torch.randn(e.shape, generator=g, **f64) * v.sqrt()
+        if camera == CAMERA_SCMOS_ADU:
+            e = e / gain[cols, rows].double() + off[cols, rows].double()
+        out.update(var=var, gain=gain, offset=off, xc=xc, yc=yc, ny=sensor, nx=sensor)
+    out["data"] = e.float().contiguous().view(-1)
+    return out

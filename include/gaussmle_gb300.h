@@ -176,6 +176,76 @@ gmle_status gmle_autotune(gmle_ctx *ctx, const gmle_fit_desc *desc, const float 
 /* Number of fit-kernel launches this context has issued (for accounting). */
 int64_t gmle_kernel_launches(const gmle_ctx *ctx);
 
+/*
+ * One homogeneous group of a mixed batch: its own fit descriptor and buffers.
+ * Pointers are device pointers for gmle_fit_mixed_device and host pointers
+ * for gmle_submit.
+ */
+typedef struct {
+    gmle_fit_desc desc;
+    const float *data;
+    const int32_t *x_corners;
+    const int32_t *y_corners;
+    int64_t n;
+    float *params;
+    float *crlb;
+    float *llr;
+    uint8_t *flags;
+} gmle_group;
+
+/*
+ * Fit a mixed batch (any mix of PSF models and box sizes 5..15) of
+ * device-resident groups with one persistent, work-stealing kernel launch per
+ * camera family present, enqueued on `stream` (used as given).  No reference
+ * counterpart: the reference fits one (model, box) per fit() call
+ * (src/interface.jl:177-291).
+ */
+gmle_status gmle_fit_mixed_device(gmle_ctx *ctx, const gmle_group *groups, int32_t ngroups,
+                                  void *stream);
+
+/*
+ * Serving loop (no reference counterpart: GaussMLE.fit is one blocking call
+ * per batch, src/interface.jl:220-262).  A scheduler thread owned by the
+ * context admits submitted requests into a device arena (admission by HBM
+ * budget, FIFO), copies their ROIs in, and continuously batches every request
+ * whose data has arrived into the next persistent mixed-batch launch; up to
+ * max_inflight_steps launches run concurrently, so requests that arrive while
+ * others are on the GPU start as soon as SMs and memory free up.  Results are
+ * copied back into the caller's host buffers, which must stay valid until
+ * the request completes.
+ */
+typedef struct {
+    int64_t hbm_budget_bytes;   /* device arena; 0 = half of the free HBM at start */
+    int32_t max_inflight_steps; /* concurrent kernel launches; 0 = 2 */
+    int64_t max_step_rois;      /* ROIs per launch; 0 = 2^21 */
+    int32_t max_pending;        /* queued requests before submit rejects; 0 = 1 << 16 */
+    int32_t use_graphs;         /* 1: each launch is a replay of a captured CUDA graph */
+} gmle_server_config;
+
+typedef struct {
+    int64_t submitted, completed, rejected, failed;
+    int64_t rois_completed;
+    int64_t steps;              /* kernel launches (graph replays) */
+    double p50_latency_ms, p99_latency_ms, mean_latency_ms, max_latency_ms;
+    double fits_per_s;          /* completed ROIs / (last completion - first submission) */
+    int64_t hbm_budget_bytes, hbm_in_use_bytes, hbm_peak_bytes;
+} gmle_server_stats;
+
+gmle_status gmle_server_start(gmle_ctx *ctx, const gmle_server_config *config);
+/* Finishes all admitted and queued work, then stops the scheduler. */
+gmle_status gmle_server_stop(gmle_ctx *ctx);
+/* Queue one request (host pointers, flags may be NULL).  GMLE_ADMISSION_REJECTED
+ * when it can never fit the arena or the queue is full. */
+gmle_status gmle_submit(gmle_ctx *ctx, const gmle_group *request, uint64_t *ticket);
+/* GMLE_OK when the request is done (its outputs are written), GMLE_NOT_READY
+ * while it runs, or the status it failed with.  A finished ticket is
+ * forgotten once GMLE_OK (or its failure) has been returned. */
+gmle_status gmle_poll(gmle_ctx *ctx, uint64_t ticket);
+/* Like gmle_poll but blocks up to timeout_ns (< 0: forever); GMLE_TIMEOUT. */
+gmle_status gmle_wait(gmle_ctx *ctx, uint64_t ticket, int64_t timeout_ns);
+/* Counters and latency percentiles since start (or the last reset). */
+gmle_status gmle_server_stats_get(gmle_ctx *ctx, gmle_server_stats *out, int32_t reset);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,167 @@
+"""GPU tests of the mixed-batch persistent kernel and the serving loop.
+
+* One persistent launch over a heterogeneous batch gives the same results as
+  the plain kernel on each group alone (same arithmetic: bit-identical).
+* Served requests give the same result alone and in a mix, and match the
+  FP32 oracle within the parity bar (tests/parity_cases.py).
+* Admission: a request that can never fit the HBM budget is rejected;
+  requests beyond the free budget queue and complete.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import gaussmle_gb300 as G
+from gaussmle_gb300 import serve
+from gaussmle_gb300.fitter import make_desc
+from oracle import oracle as O
+from parity_cases import compare, make_case, oracle_desc
+
+pytestmark = pytest.mark.gpu
+
+MIX = [("xynb-11", 0, 11, 2, 700), ("xynbs-9", 1, 9, 2, 500), ("xynbsxsy-13", 2, 13, 2, 300),
+       ("astig-15", 3, 15, 2, 300), ("xynb-7", 0, 7, 2, 130)]
+
+
+def _set_maps(ctx, maps):
+    var, gain, off = (np.asfortranarray(m) for m in maps)
+    ctx.check(ctx.lib.gmle_set_calibration(ctx.handle, var.ctypes.data_as(C.c_void_p),
+                                           gain.ctypes.data_as(C.c_void_p),
+                                           off.ctypes.data_as(C.c_void_p), var.shape[0],
+                                           var.shape[1]))
+
+
+def _cases():
+    """The mix on one shared 256x256 sensor (the maps of the first case)."""
+    ws = [make_case(*c, seed=11 + k) for k, c in enumerate(MIX)]
+    maps = ws[0].maps
+    from gaussmle_gb300 import simulate
+    out = []
+    for k, w in enumerate(ws):
+        rng = np.random.Generator(np.random.Philox(100 + k))
+        xc, yc = simulate.random_corners(rng, w.n, w.box, 256, 256)
+        data = simulate.scmos_rois(rng, w.psf, w.truth, w.box, maps, xc, yc)
+        out.append(simulate.Workload(w.name, w.psf, w.box, 2, w.constraints,
+                                     np.asfortranarray(data), xc, yc, w.truth, maps=maps))
+    return out
+
+
+def _dev(torch, w):
+    dev = torch.device("cuda", 0)
+    P = w.psf.nparams
+    t = {
+        "data": torch.from_numpy(np.ascontiguousarray(w.data.transpose(2, 1, 0)).reshape(-1)).to(dev),
+        "xc": torch.from_numpy(w.x_corners).to(dev), "yc": torch.from_numpy(w.y_corners).to(dev),
+        "params": torch.full((w.n, P), float("nan"), device=dev),
+        "crlb": torch.full((w.n, P), float("nan"), device=dev),
+        "llr": torch.full((w.n,), float("nan"), device=dev),
+        "flags": torch.zeros(w.n, dtype=torch.uint8, device=dev),
+    }
+    return t
+
+
+def test_mixed_launch_matches_plain_kernel(ctx):
+    torch = pytest.importorskip("torch")
+    ws = _cases()
+    _set_maps(ctx, ws[0].maps)
+    bufs = [_dev(torch, w) for w in ws]
+    groups = [serve.make_group(w.psf, w.box, 2, w.constraints, b["data"], b["xc"], b["yc"],
+                               b["params"], b["crlb"], b["llr"], b["flags"])
+              for w, b in zip(ws, bufs)]
+    l0 = ctx.launches()
+    serve.fit_mixed_device(ctx, groups)
+    torch.cuda.synchronize()
+    assert ctx.launches() - l0 == 1  # one persistent launch for the whole sCMOS mix
+    for w, b in zip(ws, bufs):
+        ref = _dev(torch, w)
+        ctx.check(ctx.lib.gmle_set_tuning(ctx.handle, w.psf.model_id, w.box, 2, 1, 32))
+        try:
+            G.fit_device(ctx, make_desc(w.psf, w.box, 20, w.constraints, 2), ref["data"],
+                         ref["xc"], ref["yc"], ref["params"], ref["crlb"], ref["llr"], ref["flags"])
+            torch.cuda.synchronize()
+        finally:
+            ctx.check(ctx.lib.gmle_set_tuning(ctx.handle, w.psf.model_id, w.box, 2, 0, 0))
+        for k in ("params", "crlb", "llr", "flags"):
+            a, r = b[k].cpu().numpy(), ref[k].cpu().numpy()
+            assert np.array_equal(a, r, equal_nan=True), (w.name, k, np.nanmax(np.abs(a - r)))
+
+
+def _host_bufs(w):
+    P = w.psf.nparams
+    return {"data": np.asfortranarray(w.data, np.float32), "xc": w.x_corners, "yc": w.y_corners,
+            "params": np.full((w.n, P), np.nan, np.float32),
+            "crlb": np.full((w.n, P), np.nan, np.float32),
+            "llr": np.full(w.n, np.nan, np.float32), "flags": np.zeros(w.n, np.uint8)}
+
+
+def _group(w, b):
+    return serve.make_group(w.psf, w.box, 2, w.constraints, b["data"], b["xc"], b["yc"],
+                            b["params"], b["crlb"], b["llr"], b["flags"])
+
+
+def test_served_results_same_alone_and_in_mix(ctx):
+    ws = _cases()
+    _set_maps(ctx, ws[0].maps)
+    srv = serve.Server(ctx, hbm_budget_bytes=256 << 20, max_inflight_steps=2)
+    try:
+        # alone: one request at a time
+        alone = []
+        for w in ws:
+            b = _host_bufs(w)
+            srv.wait(srv.submit(_group(w, b), keep=b), timeout_s=60)
+            alone.append(b)
+        # in the mix: all requests submitted at once (several copies of each)
+        mixed = []
+        tickets = []
+        for rep in range(3):
+            for w in ws:
+                b = _host_bufs(w)
+                tickets.append(srv.submit(_group(w, b), keep=b))
+                mixed.append(b)
+        for t in tickets:
+            srv.wait(t, timeout_s=120)
+        st = srv.stats()
+    finally:
+        srv.stop()
+    assert st["completed"] == len(ws) * 4 and st["failed"] == 0
+    assert st["p99_latency_ms"] >= st["p50_latency_ms"] > 0
+    for rep in range(3):
+        for k, w in enumerate(ws):
+            a, b = alone[k], mixed[rep * len(ws) + k]
+            for key in ("params", "crlb", "llr", "flags"):
+                assert np.array_equal(a[key], b[key], equal_nan=True), (w.name, key)
+    # and the served results meet the parity bar against the FP32 oracle
+    for w, b in zip(ws, alone):
+        ref = O.fit(oracle_desc(O, w), w.data, w.x_corners, w.y_corners, w.maps, "f32")
+        ok, s = compare(w.psf.model_id, b["params"], b["crlb"], b["flags"], ref)
+        assert s["pass_frac"] >= (0.97 if w.psf.model_id == 3 else 0.995), (w.name, s)
+
+
+def test_admission_by_hbm_budget(ctx):
+    ws = _cases()
+    _set_maps(ctx, ws[0].maps)
+    w = ws[0]
+    srv = serve.Server(ctx, hbm_budget_bytes=1 << 20, max_inflight_steps=2)
+    try:
+        big = [_host_bufs(w) for _ in range(6)]   # 700 ROIs of 11x11: ~0.4 MB fits alone
+        tickets = [srv.submit(_group(w, b), keep=b) for b in big]
+        # six of them exceed the 1 MiB arena together: they queue and all complete
+        for t in tickets:
+            srv.wait(t, timeout_s=120)
+        from gaussmle_gb300 import simulate
+        rng = np.random.Generator(np.random.Philox(5))
+        n = 4000  # ~2.2 MB: can never fit
+        xc, yc = simulate.random_corners(rng, n, 11, 256, 256)
+        huge = {"data": np.zeros((11, 11, n), np.float32, order="F"), "xc": xc, "yc": yc,
+                "params": np.zeros((n, 4), np.float32), "crlb": np.zeros((n, 4), np.float32),
+                "llr": np.zeros(n, np.float32), "flags": np.zeros(n, np.uint8)}
+        with pytest.raises(G.GaussMLEError) as ei:
+            srv.submit(_group(w, huge), keep=huge)
+        assert ei.value.status == 5  # GMLE_ADMISSION_REJECTED
+        st = srv.stats()
+        assert st["completed"] == 6 and st["rejected"] == 1
+        assert st["hbm_peak_bytes"] <= st["hbm_budget_bytes"]
+        del big
+    finally:
+        srv.stop()
