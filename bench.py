@@ -1,22 +1,27 @@
 #!/usr/bin/env python3
 """Benchmark of the batched per-ROI Gaussian MLE fit on GB300.
 
-Workload (default): GaussianXYNBS with fitted sigma (true sigma U(1.0, 1.8)),
-13x13 Float32 ROIs, 1 000 000 ROIs per step, sCMOS camera with 2048x2048
-device-resident variance / gain / offset maps, ADU data converted on the
-device, 20 Newton iterations.  Synthetic, seeded data generated on the device.
+Workload: the mixed batch - 2 000 000 ROIs per step, 40% GaussianXYNB 11x11,
+25% GaussianXYNBS 9x9, 15% GaussianXYNBSXSY 13x13, 15% AstigmaticXYZNB
+15x15, 5% GaussianXYNB 7x7, photons log-uniform 100..20000, sCMOS ADU data
+on device-resident 2048x2048 variance / gain / offset maps, 20 Newton
+iterations.  Synthetic, seeded, generated on the device.
 
-One step = one fit of the whole batch.  `value` = ROI fits/s with the inputs
-already in HBM (one kernel launch per step, CUDA events on the launch stream;
-the 676 MB of pixel data per step exceed the 129 MB L2, so no flush is
-needed).  `e2e` = the same metric through the C-ABI host-buffer call
-gmle_fit() with pinned host buffers: H2D of pixels + corners and D2H of
-params, CRLB, LLR and flags are inside the timed region.
-
-`--impl reference` times the reference's algorithm on the host cores: the
-FP32 CPU restatement of src/unified_kernel.jl (the reference is Julia, which
-is not available here), OpenMP over ROIs on all host threads, each step a
-bounded sample of the same workload.
+One step = one fit of the whole batch.
+  value  ROI fits/s of the persistent mixed-batch kernel (one work-stealing
+         launch per step) with the inputs resident in HBM; CUDA events on the
+         launch stream; 1.4 GB of pixels per step exceed the 129 MB L2.
+  e2e    the same batch through the serving API: cut into requests of
+         log-uniform 50..50000 ROIs, submitted at once with pinned host
+         buffers (gmle_submit), every H2D and D2H inside the timed region.
+  plain  the same requests through the per-batch call gmle_fit, one at a
+         time (the reference's one-launch-per-batch pattern), and the same
+         batch as one plain launch per group on device-resident data.
+  latency  p50/p99 of requests arriving as a Poisson process (served vs plain).
+`--impl reference` times the reference algorithm on the host cores: the FP32
+CPU restatement of src/unified_kernel.jl (the Julia reference is not
+installable here), OpenMP over ROIs on all host threads, each step a bounded
+sample of the same mixed batch.
 """
 from __future__ import annotations
 
@@ -36,9 +41,10 @@ sys.path.insert(0, str(ROOT / "gaussmle.jl_gb300"))
 
 import numpy as np  # noqa: E402
 
-METRIC = "ROI fits/sec on 1 GB300 (plain one-launch-per-batch kernel)"
+METRIC = "ROI fits/sec on 1 GB300 (served mixed batch vs plain kernel); p50/p99 request latency"
 UNIT = "fits/s"
-WORKLOAD = "gaussian-xynbs-13x13-scmos-1e6"
+WORKLOAD = ("mixed-batch: 40% XYNB 11x11, 25% XYNBS 9x9, 15% XYNBSXSY 13x13, "
+            "15% astigmatic 15x15, 5% XYNB 7x7; sCMOS ADU, 2048x2048 maps; 20 iterations")
 
 
 def parse():
@@ -47,13 +53,17 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--n", type=int, default=1_000_000)
+    p.add_argument("--n", type=int, default=2_000_000, help="ROIs per step")
     p.add_argument("--cpu-seconds", type=float, default=10.0,
                    help="target CPU time of the cpu_baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--shape", default=None,
-                   help="THREADS_PER_ROI,ROIS_PER_BLOCK: fixed launch shape instead of autotuning")
+    p.add_argument("--no-latency", action="store_true")
+    p.add_argument("--no-extras", action="store_true")
+    p.add_argument("--loads", default="5e6,2e7",
+                   help="offered loads (ROIs/s) of the latency measurement")
+    p.add_argument("--load-rois", type=float, default=2e7,
+                   help="ROIs of arrivals per load point (bounded to about 1.5 s)")
     return p.parse_args()
 
 
@@ -123,6 +133,7 @@ def fp32_peak_tinst(torch, dev) -> float:
         e1.synchronize()
         best = min(best, e0.elapsed_time(e1) / 1e3)
     del a, b
+    torch.cuda.empty_cache()
     return n ** 3 / best / 1e12
 
 
@@ -133,54 +144,58 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-# ---------------------------------------------------------------------------
-
-def cpu_baseline(wl_host: dict, seconds: float, threads: int = 0) -> dict:
-    """Time the FP32 CPU restatement of the reference path on a bounded sample."""
-    sys.path.insert(0, str(ROOT))
-    from oracle import oracle as O
-    from gaussmle_gb300.constraints import default_constraints
-    from gaussmle_gb300.models import GaussianXYNBS
-    cons = default_constraints(GaussianXYNBS(), 11)
-    box = wl_host["box"]
-    d = O.make_desc(1, box, 20, 2, np.zeros(8, np.float32), cons.lower, cons.upper,
-                    cons.max_step)
-    maps = wl_host["maps"]
-    data = wl_host["data"]
-    nth = threads if threads > 0 else O.max_threads()
-
-    def run(m):
-        t = time.perf_counter()
-        O.fit(d, data[:, :, :m], wl_host["xc"][:m], wl_host["yc"][:m], maps, "f32", nth)
-        return time.perf_counter() - t
-
-    m0 = min(2000, data.shape[2])
-    t0 = run(m0)
-    m = int(min(data.shape[2], max(m0, m0 * seconds / max(t0, 1e-6))))
-    t = run(m)
-    return {"value": m / t, "unit": UNIT, "cores": nth, "kind": "port",
-            "sample": f"first {m} ROIs of the workload ({t:.1f} s on {nth} host threads; "
-                      "FP32 restatement of the reference CPU path, oracle/gmle_oracle.c)"}
-
-
-def host_copy(wl: dict) -> dict:
-    """Host (numpy) copies of the device workload for the CPU paths."""
-    box, n = wl["box"], wl["n"]
-    data = wl["data"].cpu().numpy().reshape(n, box, box).transpose(2, 1, 0)
-    var = wl["var"].cpu().numpy().T
-    gain = wl["gain"].cpu().numpy().T
-    off = wl["offset"].cpu().numpy().T
-    return {"data": data, "xc": wl["xc"].cpu().numpy(), "yc": wl["yc"].cpu().numpy(),
-            "maps": (var, gain, off), "box": box, "n": n}
-
-
-# ---------------------------------------------------------------------------
-
 def dist_init():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return world, rank, local
+
+
+def set_maps(ctx, maps):
+    # (ny, nx) column-major maps are stored as row-major (nx, ny) tensors
+    v, g, o = (maps[k].cpu().numpy() for k in ("var", "gain", "offset"))
+    ctx.check(ctx.lib.gmle_set_calibration(ctx.handle, v.ctypes.data_as(C.c_void_p),
+                                           g.ctypes.data_as(C.c_void_p),
+                                           o.ctypes.data_as(C.c_void_p), maps["ny"], maps["nx"]))
+
+
+# ---------------------------------------------------------------------------
+
+def oracle_sample(groups, maps, m_total: int, threads: int):
+    """Time the FP32 CPU restatement on a proportional sample of the batch."""
+    sys.path.insert(0, str(ROOT))
+    from oracle import oracle as O
+    var, gain, off = (maps[k].cpu().numpy().T for k in ("var", "gain", "offset"))
+    n_all = sum(g["n"] for g in groups)
+    jobs = []
+    for g in groups:
+        m = max(1, int(round(m_total * g["n"] / n_all)))
+        box = g["box"]
+        data = g["data"][: m * box * box].cpu().numpy().reshape(m, box, box).transpose(2, 1, 0)
+        c = g["constraints"]
+        d = O.make_desc(g["model"], box, 20, g["camera"], g["psf"].psf_vector(), c.lower,
+                        c.upper, c.max_step)
+        jobs.append((d, data, g["xc"][:m].cpu().numpy(), g["yc"][:m].cpu().numpy(), m))
+
+    def run():
+        t = time.perf_counter()
+        for d, data, xc, yc, m in jobs:
+            O.fit(d, data, xc, yc, (var, gain, off), "f32", threads)
+        return time.perf_counter() - t
+
+    return run, sum(j[4] for j in jobs), O.max_threads()
+
+
+def cpu_baseline(groups, maps, seconds: float) -> dict:
+    run, m, nth = oracle_sample(groups, maps, 4000, 0)
+    t0 = run()
+    scale = max(1.0, seconds / max(t0, 1e-6))
+    run, m, nth = oracle_sample(groups, maps, int(4000 * scale), 0)
+    t = run()
+    return {"value": m / t, "unit": UNIT, "cores": nth, "kind": "port",
+            "sample": f"{m} ROIs of the mixed batch, in its proportions ({t:.1f} s on {nth} "
+                      "host threads; FP32 restatement of the reference CPU path, "
+                      "oracle/gmle_oracle.c)"}
 
 
 def run_reference(args):
@@ -190,43 +205,95 @@ def run_reference(args):
     import torch
     from gaussmle_gb300 import simulate
     dev = "cuda:0" if torch.cuda.is_available() else "cpu"
-    wl = simulate.config1_device(n=min(args.n, 200_000), device=dev)
-    host = host_copy(wl)
-    sys.path.insert(0, str(ROOT))
-    from oracle import oracle as O
-    from gaussmle_gb300.constraints import default_constraints
-    from gaussmle_gb300.models import GaussianXYNBS
-    cons = default_constraints(GaussianXYNBS(), 11)
-    d = O.make_desc(1, 13, 20, 2, np.zeros(8, np.float32), cons.lower, cons.upper, cons.max_step)
-    nth = O.max_threads()
+    maps, groups = simulate.config3_device(n=min(args.n, 200_000), device=dev)
     per_step = 20_000
-    data = host["data"]
-
-    def step(k):
-        lo = (k * per_step) % (data.shape[2] - per_step)
-        O.fit(d, data[:, :, lo:lo + per_step], host["xc"][lo:lo + per_step],
-              host["yc"][lo:lo + per_step], host["maps"], "f32", nth)
-
-    for k in range(args.warmup):
-        step(k)
+    run, m, nth = oracle_sample(groups, maps, per_step, 0)
+    for _ in range(args.warmup):
+        run()
     t = time.perf_counter()
-    for k in range(args.steps):
-        step(args.warmup + k)
+    for _ in range(args.steps):
+        run()
     dt = time.perf_counter() - t
-    value = per_step * args.steps / dt
-    sample = (f"{per_step} ROIs of the workload per step on {nth} host threads "
-              "(FP32 restatement of the reference CPU path, oracle/gmle_oracle.c; "
-              "the Julia reference is not installable here)")
+    value = m * args.steps / dt
+    sample = (f"{m} ROIs of the mixed batch per step on {nth} host threads (FP32 restatement "
+              "of the reference CPU path, oracle/gmle_oracle.c; the Julia reference is not "
+              "installable here)")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "rois_per_step": per_step, "iterations": 20},
+        "config": {"workload": WORKLOAD, "rois_per_step": m, "iterations": 20},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
+
+
+# ---------------------------------------------------------------------------
+
+def device_groups(torch, groups, dev):
+    from gaussmle_gb300 import serve
+    out = []
+    for g in groups:
+        n, P = g["n"], g["psf"].nparams
+        b = {"params": torch.empty((n, P), device=dev), "crlb": torch.empty((n, P), device=dev),
+             "llr": torch.empty(n, device=dev), "flags": torch.empty(n, dtype=torch.uint8,
+                                                                        device=dev)}
+        b["group"] = serve.make_group(g["psf"], g["box"], g["camera"], g["constraints"],
+                                      g["data"], g["xc"], g["yc"], b["params"], b["crlb"],
+                                      b["llr"], b["flags"])
+        out.append(b)
+    return out
+
+
+def time_steps(torch, stream, fn, steps, warmup):
+    for _ in range(max(warmup, 3)):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def extras(torch, ctx, dev, steps):
+    """Plain-kernel throughput of the other workloads (device-resident)."""
+    import gaussmle_gb300 as G
+    from gaussmle_gb300 import simulate, roofline
+    from gaussmle_gb300.fitter import make_desc
+    out = {}
+    stream = torch.cuda.Stream(dev)
+    for name, model, box, cam, n in [("xynb-11x11-poisson-10k (reference CPU case)", 0, 11, 0, 10_000),
+                                     ("xynb-11x11-poisson-1e6", 0, 11, 0, 1_000_000),
+                                     ("xynbs-13x13-scmos-1e6", 1, 13, 2, 1_000_000),
+                                     ("astig-15x15-poisson-1e6", 3, 15, 0, 1_000_000)]:
+        wl = simulate.device_workload(model, box, cam, n, device=dev)
+        if cam:
+            set_maps(ctx, wl)
+        psf, P = wl["psf"], wl["psf"].nparams
+        cons = simulate.ASTIG_WIDE if model == 3 else G.default_constraints(psf, 11)
+        desc = make_desc(psf, box, 20, cons, cam)
+        prm = torch.empty((n, P), device=dev)
+        crl = torch.empty((n, P), device=dev)
+        llr = torch.empty(n, device=dev)
+        flg = torch.empty(n, dtype=torch.uint8, device=dev)
+        from gaussmle_gb300 import tuning
+        tpr, rpb, _ = tuning.autotune(ctx, desc, wl["data"], wl["xc"], wl["yc"], prm, crl, llr,
+                                      flg, save=False)
+        dt = time_steps(torch, stream, lambda: G.fit_device(ctx, desc, wl["data"], wl["xc"],
+                                                             wl["yc"], prm, crl, llr, flg,
+                                                             stream=stream), steps, 3)
+        per = dt / steps
+        w = roofline.work_per_roi(model, box, 20, cam)
+        out[name] = {"fits_per_s": n / per, "ms_per_launch": per * 1e3,
+                     "shape": [tpr, rpb], "work_fp32_equiv_per_roi": w["fp32_equiv"]}
+        del wl, prm, crl, llr, flg
+        torch.cuda.empty_cache()
+    return out
 
 
 def run_ours(args):
@@ -239,58 +306,30 @@ def run_ours(args):
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     import gaussmle_gb300 as G
-    from gaussmle_gb300 import simulate, roofline
-    from gaussmle_gb300.fitter import make_desc
+    from gaussmle_gb300 import simulate, roofline, serve, loadgen
 
     n = args.n
-    wl = simulate.config1_device(n=n, seed=1001 + rank, device=dev)
+    maps, groups = simulate.config3_device(n=n, seed=1003 + rank, device=dev)
     ctx = G.Context(local)
-    desc = make_desc(G.GaussianXYNBS(), 13, 20, G.default_constraints(G.GaussianXYNBS(), 11), 2)
-    # calibration maps: device-resident, uploaded once
-    var_h, gain_h, off_h = (wl[k].cpu().numpy() for k in ("var", "gain", "offset"))
-    ctx.check(ctx.lib.gmle_set_calibration(ctx.handle, var_h.ctypes.data_as(C.c_void_p),
-                                           gain_h.ctypes.data_as(C.c_void_p),
-                                           off_h.ctypes.data_as(C.c_void_p), wl["ny"], wl["nx"]))
-    P = 5
-    params = torch.empty((n, P), device=dev)
-    crlb = torch.empty((n, P), device=dev)
-    llr = torch.empty(n, device=dev)
-    flags = torch.empty(n, dtype=torch.uint8, device=dev)
-    stream = torch.cuda.Stream(dev)   # the launch stream; events are recorded on it
+    set_maps(ctx, maps)
+    dgs = device_groups(torch, groups, dev)
+    gstructs = [b["group"] for b in dgs]
+    stream = torch.cuda.Stream(dev)
 
+    # ---- value: one persistent work-stealing launch per step ----
     def step():
-        G.fit_device(ctx, desc, wl["data"], wl["xc"], wl["yc"], params, crlb, llr, flags,
-                     stream=stream)
-
-    # launch shape chosen by the project's autotuner (untimed), or fixed by --shape
-    from gaussmle_gb300 import tuning
-    if args.shape:
-        tpr, rpb = (int(v) for v in args.shape.split(","))
-        ctx.check(ctx.lib.gmle_set_tuning(ctx.handle, 1, 13, 2, tpr, rpb))
-        tune = (tpr, rpb, None)
-    else:
-        tune = tuning.autotune(ctx, desc, wl["data"], wl["xc"], wl["yc"], params, crlb, llr,
-                               flags, save=False)
+        serve.fit_mixed_device(ctx, gstructs, stream=stream)
 
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
-    # time of one launch alone (for the roofline; same stream, events around it)
-    a0 = torch.cuda.Event(enable_timing=True)
-    a1 = torch.cuda.Event(enable_timing=True)
-    a0.record(stream)
-    step()
-    a1.record(stream)
-    torch.cuda.synchronize()
-    single_launch_s = a0.elapsed_time(a1) / 1e3
     launches0 = ctx.launches()
     sampler = ClockSampler(local)
     sampler.start()
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(args.steps):
         step()
@@ -306,78 +345,107 @@ def run_ours(args):
     launches = ctx.launches() - launches0
     value = n * args.steps * world / dt
     per_launch = dt / args.steps
-    conv = float((flags.cpu().numpy() & 1).mean())
+    conv = float(np.mean([(b["flags"].cpu().numpy() & 1).mean() for b in dgs]))
 
-    # ---- end to end through the C-ABI host-buffer call (pinned host memory) ----
-    e2e = None
-    if not args.no_e2e:
-        h_data = wl["data"].cpu().pin_memory()
-        h_xc = wl["xc"].cpu().pin_memory()
-        h_yc = wl["yc"].cpu().pin_memory()
-        h_par = torch.empty((n, P), pin_memory=True)
-        h_crlb = torch.empty((n, P), pin_memory=True)
-        h_llr = torch.empty(n, pin_memory=True)
-        h_fl = torch.empty(n, dtype=torch.uint8, pin_memory=True)
-        vp = lambda t: C.c_void_p(t.data_ptr())
+    # ---- plain kernel on the same device-resident batch: one launch per group ----
+    from gaussmle_gb300.fitter import make_desc
+    from gaussmle_gb300 import tuning
 
-        def host_step():
-            ctx.check(ctx.lib.gmle_fit(ctx.handle, C.byref(desc), vp(h_data), vp(h_xc), vp(h_yc),
-                                       n, vp(h_par), vp(h_crlb), vp(h_llr), vp(h_fl)))
-        for _ in range(max(args.warmup, 3)):
-            host_step()
-        l0 = ctx.launches()
-        if world > 1:
-            dist.barrier()
-        t = time.perf_counter()
-        for _ in range(args.steps):
-            host_step()
-        et = time.perf_counter() - t
-        if world > 1:
-            tt = torch.tensor([et], device=dev, dtype=torch.float64)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            et = float(tt.item())
-        e2e = {"value": n * args.steps * world / et, "unit": UNIT,
-               "h2d_bytes_per_step": n * (13 * 13 * 4 + 8),
-               "d2h_bytes_per_step": n * (2 * P * 4 + 4 + 1),
-               "gpu_launches": ctx.launches() - l0,
-               "ms_per_step": et / args.steps * 1e3}
+    def plain_step():
+        for g, b in zip(groups, dgs):
+            G.fit_device(ctx, b["group"].desc, g["data"], g["xc"], g["yc"], b["params"],
+                         b["crlb"], b["llr"], b["flags"], stream=stream)
+    for g, b in zip(groups, dgs):
+        tuning.autotune(ctx, b["group"].desc, g["data"], g["xc"], g["yc"], b["params"],
+                        b["crlb"], b["llr"], b["flags"], save=False)
+    dt_plain_dev = time_steps(torch, stream, plain_step, args.steps, 3)
+
+    # ---- e2e: served requests (pinned host buffers) vs per-request plain calls ----
+    e2e, plain, latency = None, None, None
+    if not args.no_e2e or not args.no_latency:
+        pools = loadgen.HostPools(groups)
+        reqs = loadgen.make_stream(pools, n, seed=7 + rank)
+        srv = serve.Server(ctx, max_inflight_steps=4)
+        try:
+            if not args.no_e2e:
+                for _ in range(max(1, min(args.warmup, 2))):
+                    loadgen.run_batch_served(srv, pools, reqs)
+                srv.stats(reset=True)
+                l0 = ctx.launches()
+                ts = [loadgen.run_batch_served(srv, pools, reqs) for _ in range(args.steps)]
+                st = srv.stats()
+                et = sum(ts)
+                h2d = sum(r.n * (groups[r.group]["box"] ** 2 * 4 + 8) for r in reqs)
+                d2h = sum(r.n * (2 * groups[r.group]["psf"].nparams * 4 + 5) for r in reqs)
+                e2e = {"value": n * args.steps * world / et, "unit": UNIT,
+                       "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                       "gpu_launches": ctx.launches() - l0, "ms_per_step": et / args.steps * 1e3,
+                       "requests_per_step": len(reqs), "api": "gmle_submit / gmle_wait",
+                       "server_p50_ms": st["p50_latency_ms"], "server_p99_ms": st["p99_latency_ms"]}
+                loadgen.run_batch_plain(ctx, pools, reqs[:50])
+                tp = loadgen.run_batch_plain(ctx, pools, reqs)
+                plain = {"per_request_gmle_fit": {"value": n / tp, "unit": UNIT,
+                                                  "ms_per_step": tp * 1e3,
+                                                  "api": "gmle_fit per request"},
+                         "one_launch_per_group_device": {"value": n * args.steps / dt_plain_dev,
+                                                         "unit": UNIT}}
+            if not args.no_latency:
+                latency = {"served": [], "plain": []}
+                for load in [float(x) for x in args.loads.split(",")]:
+                    tot = min(args.load_rois, load * 1.5)
+                    lreqs = loadgen.make_stream(pools, int(tot), seed=13)
+                    latency["served"].append(loadgen.run_stream_served(srv, pools, lreqs, load))
+                    latency["plain"].append(loadgen.run_stream_plain(ctx, pools, lreqs, load))
+        finally:
+            srv.stop()
 
     if rank != 0:
         return
-    # ---- roofline: issue-bound FP32 + SFU work vs the measured FP32 rate ----
-    w = roofline.work_per_roi(1, 13, 20, 2)
-    peak_inst = fp32_peak_tinst(torch, dev)  # T lane-inst/s
-    achieved = w["fp32_equiv"] * n / per_launch / 1e12  # per launch, averaged over the K steps
+    # ---- roofline of the mixed kernel: issue-bound FP32 + SFU + FP64 work ----
+    work = sum(g["n"] * roofline.work_per_roi(g["model"], g["box"], 20, g["camera"])["fp32_equiv"]
+               for g in groups)
+    bytes_ = sum(g["n"] * roofline.bytes_per_roi(g["model"], g["box"], g["camera"])
+                 for g in groups)
+    peak_inst = fp32_peak_tinst(torch, dev)
+    achieved = work / per_launch / 1e12
     peaks = measured_peaks()
-    bpr = roofline.bytes_per_roi(1, 13, 2)
-    hbm_ach = bpr * n / per_launch / 1e9
+    hbm_ach = bytes_ / per_launch / 1e9
     rl = {
         "bound": "fp32+sfu", "achieved": achieved, "peak": peak_inst, "unit": "Tinst/s",
         "frac": achieved / peak_inst, "traffic": None,
-        "peak_source": "measured in this run: FP32 SGEMM 8192^3 (TF32 off) FFMA rate",
-        "work_per_roi_fp32_equiv": w["fp32_equiv"], "single_launch_ms": single_launch_s * 1e3,
+        "kernel": "fit_mixed_kernel<true> (persistent mixed batch)",
+        "peak_source": "measured in this run: FP32 SGEMM 8192^3 (TF32 off), FFMA lane rate",
+        "work_per_step_fp32_equiv": work,
         "hbm": {"achieved_gbs": hbm_ach, "peak_gbs": peaks.get("hbm_gbs"),
-                "frac": hbm_ach / peaks.get("hbm_gbs", 6800.0), "bytes_per_roi": bpr,
+                "frac": hbm_ach / peaks.get("hbm_gbs", 6800.0), "bytes_per_step": bytes_,
                 "peak_source": "MEASURED_PEAKS.json" if "source" not in peaks else "fallback"},
     }
     cpu = None
     if not args.no_cpu_baseline and world == 1:
-        cpu = cpu_baseline(host_copy(wl), args.cpu_seconds)
+        cpu = cpu_baseline(groups, maps, args.cpu_seconds)
+    ext = None
+    if not args.no_extras and world == 1:
+        del dgs
+        torch.cuda.empty_cache()
+        ext = extras(torch, ctx, dev, max(3, args.steps // 2))
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": per_launch * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "rois_per_step": n, "box": 13, "model": "GaussianXYNBS",
-                   "camera": "sCMOS (ADU, device-side conversion)", "iterations": 20,
-                   "parallelism": f"roi-shard x{world}", "l2": "inputs (676 MB/step) > L2",
-                   "tuning": {"threads_per_roi": tune[0], "rois_per_block": tune[1],
-                              "source": "--shape" if args.shape else "gmle_autotune"}},
+        "config": {"workload": WORKLOAD, "rois_per_step": n,
+                   "groups": [{"model": g["psf"].__class__.__name__, "box": g["box"],
+                               "n": g["n"]} for g in groups],
+                   "parallelism": f"roi-shard x{world}",
+                   "l2": "inputs (~1.4 GB/step) larger than L2"},
         "gpu_launches": launches,
         "converged_fraction": conv,
         "clocks": clocks,
         "roofline": rl,
         "e2e": e2e,
+        "plain": plain,
+        "latency": latency,
         "cpu_baseline": cpu,
+        "extras": ext,
     }
     print(json.dumps(out))
 

@@ -3,13 +3,14 @@
 // A mixed batch is a list of homogeneous groups (a serving request, or one
 // (model, box) class of a heterogeneous batch), each with its own fit
 // descriptor and device buffers.  The groups' ROIs are cut into tiles of
-// `rois_per_tile` ROIs (one warp-sized block of one-thread-per-ROI fits).  A
-// persistent grid of one-warp CTAs pulls tile indices from a global atomic
-// counter (work stealing), finds the tile's group and runs the fit
-// specialised for the group's (model, box) on it; tiles of the most expensive
-// groups come first so that the tail is short.  ROI sizes 5..15 px and all
-// four PSF models share the launch; the camera family (Poisson or sCMOS) is a
-// template parameter, so a batch with both families takes two launches.
+// `rois_per_tile` ROIs (a block of one-thread-per-ROI fits).  A persistent
+// grid of CTAs pulls tile indices from a global atomic counter (work
+// stealing), finds the tile's group and runs the fit specialised for the
+// group's (model, box) on it; tiles of the most expensive groups come first
+// so that the tail is short.  All four PSF models and every box of a
+// shared-memory class share a launch; the camera family (Poisson or sCMOS)
+// and the class are template parameters, so a batch takes one launch per
+// (family, class) present, the classes of a family running concurrently.
 #pragma once
 
 #include "gmle_fit_kernel.cuh"
@@ -50,26 +51,41 @@ __device__ __noinline__ void mixed_tile(const KernelArgs a, int64_t roi0, int nr
     fit_rois_r1<MODEL, BOX, SCMOS>(a, roi0, nroi, smem);
 }
 
-template <bool SCMOS>
+// Shared-memory classes: ROIs up to 9x9, 11x11, and 13x13 or 15x15.  Each
+// class has its own persistent kernel (so that its register allocation is
+// that of its own box sizes) and tile size.
+__host__ __device__ constexpr int box_class(int box) { return box <= 9 ? 0 : (box <= 11 ? 1 : 2); }
+__host__ __device__ constexpr int class_tile(int cls) { return cls == 2 ? 32 : 64; }
+
+template <bool SCMOS, int CLASS>
 __device__ void mixed_dispatch(int model, int box, const KernelArgs &a, int64_t roi0, int nroi,
                                float *smem)
 {
 #define GMLE_MX(M, B) \
     case (M) * 32 + (B): mixed_tile<M, B, SCMOS>(a, roi0, nroi, smem); break;
-#define GMLE_MXM(M) GMLE_MX(M, 5) GMLE_MX(M, 7) GMLE_MX(M, 9) GMLE_MX(M, 11) GMLE_MX(M, 13) GMLE_MX(M, 15)
-    switch (model * 32 + box) {
-        GMLE_MXM(0)
-        GMLE_MXM(1)
-        GMLE_MXM(2)
-        GMLE_MXM(3)
-        default: break;
+    if (CLASS == 0) {
+        switch (model * 32 + box) {
+            GMLE_MX(0, 5) GMLE_MX(0, 7) GMLE_MX(0, 9) GMLE_MX(1, 5) GMLE_MX(1, 7) GMLE_MX(1, 9)
+            GMLE_MX(2, 5) GMLE_MX(2, 7) GMLE_MX(2, 9) GMLE_MX(3, 5) GMLE_MX(3, 7) GMLE_MX(3, 9)
+            default: break;
+        }
+    } else if (CLASS == 1) {
+        switch (model * 32 + box) {
+            GMLE_MX(0, 11) GMLE_MX(1, 11) GMLE_MX(2, 11) GMLE_MX(3, 11)
+            default: break;
+        }
+    } else {
+        switch (model * 32 + box) {
+            GMLE_MX(0, 13) GMLE_MX(0, 15) GMLE_MX(1, 13) GMLE_MX(1, 15)
+            GMLE_MX(2, 13) GMLE_MX(2, 15) GMLE_MX(3, 13) GMLE_MX(3, 15)
+            default: break;
+        }
     }
-#undef GMLE_MXM
 #undef GMLE_MX
 }
 
-template <bool SCMOS>
-__global__ void __launch_bounds__(32) fit_mixed_kernel(const MixedArgs m)
+template <bool SCMOS, int CLASS>
+__global__ void __launch_bounds__(64) fit_mixed_kernel(const MixedArgs m)
 {
     extern __shared__ __align__(16) float smem[];
     __shared__ long long s_tile;
@@ -117,28 +133,27 @@ __global__ void __launch_bounds__(32) fit_mixed_kernel(const MixedArgs m)
         const int64_t roi0 = (tile - G.tile0) * m.rois_per_tile;
         const int64_t left = G.n - roi0;
         const int nroi = left < m.rois_per_tile ? (int)left : m.rois_per_tile;
-        mixed_dispatch<SCMOS>(G.model, G.box, a, roi0, nroi, smem);
+        mixed_dispatch<SCMOS, CLASS>(G.model, G.box, a, roi0, nroi, smem);
         __syncthreads();  // the tile's shared memory is free again
     }
 }
 
-cudaError_t launch_mixed_poisson(const MixedArgs &m, size_t smem, int grid, cudaStream_t s);
-cudaError_t launch_mixed_scmos(const MixedArgs &m, size_t smem, int grid, cudaStream_t s);
-int mixed_blocks_per_sm_poisson(size_t smem);
-int mixed_blocks_per_sm_scmos(size_t smem);
+// Launch with rois_per_tile (= block size) threads; the class picks the kernel.
+cudaError_t launch_mixed_poisson(int cls, const MixedArgs &m, size_t smem, int grid, cudaStream_t s);
+cudaError_t launch_mixed_scmos(int cls, const MixedArgs &m, size_t smem, int grid, cudaStream_t s);
+int mixed_blocks_per_sm_poisson(int cls, size_t smem);
+int mixed_blocks_per_sm_scmos(int cls, size_t smem);
 
-inline cudaError_t launch_mixed(bool scmos, const MixedArgs &m, size_t smem, int grid,
+inline cudaError_t launch_mixed(bool scmos, int cls, const MixedArgs &m, size_t smem, int grid,
                                 cudaStream_t s)
 {
-    return scmos ? launch_mixed_scmos(m, smem, grid, s) : launch_mixed_poisson(m, smem, grid, s);
+    return scmos ? launch_mixed_scmos(cls, m, smem, grid, s)
+                 : launch_mixed_poisson(cls, m, smem, grid, s);
 }
-inline int mixed_blocks_per_sm(bool scmos, size_t smem)
+inline int mixed_blocks_per_sm(bool scmos, int cls, size_t smem)
 {
-    return scmos ? mixed_blocks_per_sm_scmos(smem) : mixed_blocks_per_sm_poisson(smem);
+    return scmos ? mixed_blocks_per_sm_scmos(cls, smem) : mixed_blocks_per_sm_poisson(cls, smem);
 }
-
-// ROIs per tile of the mixed kernel (one warp per CTA, one thread per ROI).
-constexpr int kMixedTile = 32;
 
 // Dynamic shared memory the mixed kernel may request: well under the 227 KiB
 // per-block limit, which also has to hold the kernel's static tile index (a

@@ -1,32 +1,45 @@
-// Persistent mixed-batch kernel for the scmos camera family; see gmle_mixed.cuh.
+// Persistent mixed-batch kernels for the scmos camera family; see gmle_mixed.cuh.
 #include "gmle_mixed.cuh"
 
 namespace gmle {
 
-static bool attr_done = false;
+namespace {
 
-static cudaError_t ensure_attr()
+using KernelFn = void (*)(const MixedArgs);
+
+KernelFn kernel_of(int cls)
 {
-    if (attr_done) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(fit_mixed_kernel<true>,
+    return cls == 0 ? fit_mixed_kernel<true, 0>
+                    : (cls == 1 ? fit_mixed_kernel<true, 1> : fit_mixed_kernel<true, 2>);
+}
+
+bool attr_done[3] = {false, false, false};
+
+cudaError_t ensure_attr(int cls)
+{
+    if (attr_done[cls]) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(kernel_of(cls),
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, kMixedMaxSmem);
-    if (e == cudaSuccess) attr_done = true;
+    if (e == cudaSuccess) attr_done[cls] = true;
     return e;
 }
 
-cudaError_t launch_mixed_scmos(const MixedArgs &m, size_t smem, int grid, cudaStream_t s)
+}  // namespace
+
+cudaError_t launch_mixed_scmos(int cls, const MixedArgs &m, size_t smem, int grid, cudaStream_t s)
 {
-    cudaError_t e = ensure_attr();
+    if (cls < 0 || cls > 2) return cudaErrorInvalidValue;
+    cudaError_t e = ensure_attr(cls);
     if (e != cudaSuccess) return e;
-    fit_mixed_kernel<true><<<grid, m.rois_per_tile, smem, s>>>(m);
+    kernel_of(cls)<<<grid, m.rois_per_tile, smem, s>>>(m);
     return cudaGetLastError();
 }
 
-int mixed_blocks_per_sm_scmos(size_t smem)
+int mixed_blocks_per_sm_scmos(int cls, size_t smem)
 {
+    if (cls < 0 || cls > 2 || ensure_attr(cls) != cudaSuccess) return 0;
     int nb = 0;
-    if (ensure_attr() != cudaSuccess) return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fit_mixed_kernel<true>, 32, smem) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel_of(cls), class_tile(cls), smem) !=
         cudaSuccess)
         return 0;
     return nb;

@@ -292,7 +292,7 @@ void gmle_destroy(gmle_ctx *ctx)
     if (ctx->s_d2h) cudaStreamSynchronize(ctx->s_d2h);
     server_destroy(ctx);
     for (Slot &s : ctx->slots) free_slot(s);
-    for (MixedBufs &b : ctx->mixed) free_mixed(b);
+    free_mixed_set(ctx->mixed);
     cudaFree(ctx->d_var);
     cudaFree(ctx->d_gain);
     cudaFree(ctx->d_offset);
@@ -584,16 +584,22 @@ gmle_status ensure_mixed(gmle_ctx *ctx, MixedBufs &b, int ngroups)
 {
     if (!b.reuse) {
         CK(cudaEventCreateWithFlags(&b.reuse, cudaEventDisableTiming), "cudaEventCreate");
-        CK(cudaMallocHost(&b.h_header, 2 * sizeof(int64_t)), "cudaMallocHost(header)");
         CK(cudaMalloc(&b.d_counter, sizeof(unsigned long long)), "cudaMalloc(counter)");
     }
     if (b.cap < ngroups) {
         CK(cudaEventSynchronize(b.reuse), "cudaEventSynchronize");
-        cudaFreeHost(b.h_groups);
-        b.h_groups = nullptr;
+        cudaFreeHost(b.h_base);
+        cudaFree(b.d_base);
+        b.h_base = b.d_base = nullptr;
         b.cap = 0;
         const int cap = std::max(64, ngroups);
-        CK(cudaMallocHost(&b.h_groups, sizeof(gmle::GroupDesc) * cap), "cudaMallocHost(groups)");
+        const size_t bytes = kTableHeader + sizeof(gmle::GroupDesc) * cap;
+        CK(cudaMallocHost(&b.h_base, bytes), "cudaMallocHost(group table)");
+        CK(cudaMalloc(&b.d_base, bytes), "cudaMalloc(group table)");
+        b.h_header = reinterpret_cast<int64_t *>(b.h_base);
+        b.d_header = reinterpret_cast<int64_t *>(b.d_base);
+        b.h_groups = reinterpret_cast<gmle::GroupDesc *>(b.h_base + kTableHeader);
+        b.d_groups = reinterpret_cast<gmle::GroupDesc *>(b.d_base + kTableHeader);
         b.cap = cap;
     }
     return GMLE_OK;
@@ -602,21 +608,21 @@ gmle_status ensure_mixed(gmle_ctx *ctx, MixedBufs &b, int ngroups)
 gmle_status free_mixed(MixedBufs &b)
 {
     if (b.reuse) cudaEventSynchronize(b.reuse);
-    cudaFreeHost(b.h_groups);
-    cudaFreeHost(b.h_header);
+    cudaFreeHost(b.h_base);
+    cudaFree(b.d_base);
     cudaFree(b.d_counter);
     if (b.reuse) cudaEventDestroy(b.reuse);
     b = MixedBufs();
     return GMLE_OK;
 }
 
-size_t mixed_smem(const gmle_group *groups, int32_t ngroups, bool scmos)
+size_t mixed_smem(const gmle_group *groups, int32_t ngroups, bool scmos, int tile)
 {
     size_t m = 0;
     for (int k = 0; k < ngroups; k++) {
         const gmle_fit_desc &d = groups[k].desc;
         if ((d.camera != GMLE_CAMERA_POISSON) != scmos || groups[k].n <= 0) continue;
-        m = std::max(m, gmle::smem_bytes(d.model, d.box, scmos, 1, gmle::kMixedTile));
+        m = std::max(m, gmle::smem_bytes(d.model, d.box, scmos, 1, tile));
     }
     return m;
 }
@@ -640,7 +646,7 @@ gmle_status validate_groups(gmle_ctx *ctx, const gmle_group *groups, int32_t ngr
 }
 
 int64_t build_mixed_table(gmle_ctx *ctx, const gmle_group *groups, int32_t ngroups, bool scmos,
-                          MixedBufs &b, gmle_status *st)
+                          int tile, MixedBufs &b, gmle_status *st)
 {
     *st = GMLE_OK;
     std::vector<int> idx;
@@ -679,58 +685,147 @@ int64_t build_mixed_table(gmle_ctx *ctx, const gmle_group *groups, int32_t ngrou
         std::memcpy(D.upper, G.desc.upper, sizeof D.upper);
         std::memcpy(D.max_step, G.desc.max_step, sizeof D.max_step);
         D.tile0 = tiles;
-        tiles += (G.n + gmle::kMixedTile - 1) / gmle::kMixedTile;
+        tiles += (G.n + tile - 1) / tile;
     }
     b.h_header[0] = (int64_t)idx.size();
     b.h_header[1] = tiles;
     return tiles;
 }
 
-int mixed_grid(gmle_ctx *ctx, bool scmos, size_t smem)
+int mixed_grid(gmle_ctx *ctx, bool scmos, int cls, size_t smem)
 {
-    return ctx->num_sms * std::max(1, gmle::mixed_blocks_per_sm(scmos, smem));
+    return ctx->num_sms * std::max(1, gmle::mixed_blocks_per_sm(scmos, cls, smem));
 }
 
-gmle_status enqueue_mixed(gmle_ctx *ctx, bool scmos, MixedBufs &b, size_t smem, int grid,
-                          cudaStream_t s)
+gmle_status enqueue_mixed(gmle_ctx *ctx, bool scmos, int cls, MixedBufs &b, size_t smem, int grid,
+                          cudaStream_t s, bool zero_copy)
 {
-    // The kernel reads the group table straight from pinned host memory (a
-    // few hundred bytes per tile of 32 ROIs), so a launch needs no table copy
-    // and a captured graph stays valid for any table contents.
+    // The table sits at fixed device addresses (copied in by upload_plan), so
+    // a captured graph of these launches stays valid for any table contents.
     CK(cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned long long), s), "reset tile counter");
     gmle::MixedArgs m;
-    m.groups = b.h_groups;
-    m.header = b.h_header;
+    m.groups = zero_copy ? b.h_groups : b.d_groups;
+    m.header = zero_copy ? b.h_header : b.d_header;
     m.tile_counter = b.d_counter;
     m.var = ctx->d_var;
     m.gain = ctx->d_gain;
     m.offset = ctx->d_offset;
     m.ny = ctx->ny;
     m.nx = ctx->nx;
-    m.rois_per_tile = gmle::kMixedTile;
+    m.rois_per_tile = gmle::class_tile(cls);
     m.sqrt2pi = sqrtf(2.0f * (float)3.14159265358979323846);
     m.bad_corners = ctx->d_bad;
-    CK(gmle::launch_mixed(scmos, m, smem, grid, s), "mixed kernel launch");
+    CK(gmle::launch_mixed(scmos, cls, m, smem, grid, s), "mixed kernel launch");
     return GMLE_OK;
 }
 
-gmle_status run_mixed(gmle_ctx *ctx, const gmle_group *groups, int32_t ngroups, cudaStream_t s,
-                      MixedBufs *bufs)
+gmle_status init_mixed_set(gmle_ctx *ctx, MixedSet &m)
+{
+    if (m.ev_fork) return GMLE_OK;
+    for (int c = 0; c < kClasses; c++) {
+        CK(cudaStreamCreateWithFlags(&m.fork[c], cudaStreamNonBlocking), "cudaStreamCreate");
+        CK(cudaEventCreateWithFlags(&m.ev_join[c], cudaEventDisableTiming), "cudaEventCreate");
+    }
+    CK(cudaEventCreateWithFlags(&m.ev_fork, cudaEventDisableTiming), "cudaEventCreate");
+    return GMLE_OK;
+}
+
+void free_mixed_set(MixedSet &m)
+{
+    for (int f = 0; f < 2; f++)
+        for (int c = 0; c < kClasses; c++) free_mixed(m.bufs[f][c]);
+    for (int c = 0; c < kClasses; c++) {
+        if (m.fork[c]) {
+            cudaStreamSynchronize(m.fork[c]);
+            cudaStreamDestroy(m.fork[c]);
+        }
+        if (m.ev_join[c]) cudaEventDestroy(m.ev_join[c]);
+    }
+    if (m.ev_fork) cudaEventDestroy(m.ev_fork);
+    m = MixedSet();
+}
+
+gmle_status plan_mixed(gmle_ctx *ctx, const gmle_group *groups, int32_t ngroups, MixedSet &m,
+                       MixedPlan &plan, bool allow_plain)
 {
     gmle_status st = validate_groups(ctx, groups, ngroups);
     if (st != GMLE_OK) return st;
+    plan = MixedPlan();
+    std::vector<gmle_group> sub;
+    for (int k = 0; k < ngroups; k++)
+        if (allow_plain && groups[k].n >= kPlainGroupRois) plan.plain.push_back(groups[k]);
     for (int fam = 0; fam < 2; fam++) {
         const bool scmos = fam == 1;
-        MixedBufs &b = bufs[fam];
-        const int64_t tiles = build_mixed_table(ctx, groups, ngroups, scmos, b, &st);
-        if (st != GMLE_OK) return st;
-        if (tiles == 0) continue;
-        const size_t smem = mixed_smem(groups, ngroups, scmos);
-        const int grid = (int)std::min<int64_t>(mixed_grid(ctx, scmos, smem), tiles);
-        ctx->launches++;
-        st = enqueue_mixed(ctx, scmos, b, smem, grid, s);
-        if (st != GMLE_OK) return st;
-        CK(cudaEventRecord(b.reuse, s), "cudaEventRecord");  // the table may be rewritten after this
+        for (int c = 0; c < kClasses; c++) {
+            sub.clear();
+            for (int k = 0; k < ngroups; k++)
+                if (box_class(groups[k].desc.box) == c &&
+                    !(allow_plain && groups[k].n >= kPlainGroupRois))
+                    sub.push_back(groups[k]);
+            if (sub.empty()) continue;
+            const int tile = class_tile(c);
+            const int64_t tiles = build_mixed_table(ctx, sub.data(), (int32_t)sub.size(), scmos,
+                                                    tile, m.bufs[fam][c], &st);
+            if (st != GMLE_OK) return st;
+            if (tiles == 0) continue;
+            plan.tiles[fam][c] = tiles;
+            plan.smem[fam][c] = mixed_smem(sub.data(), (int32_t)sub.size(), scmos, tile);
+            plan.grid[fam][c] = mixed_grid(ctx, scmos, c, plan.smem[fam][c]);
+        }
+    }
+    return GMLE_OK;
+}
+
+gmle_status upload_plan(gmle_ctx *ctx, MixedSet &m, const MixedPlan &plan, cudaStream_t s,
+                        bool record_reuse)
+{
+    if (m.zero_copy) return GMLE_OK;
+    for (int fam = 0; fam < 2; fam++)
+        for (int c = 0; c < kClasses; c++) {
+            if (plan.tiles[fam][c] == 0) continue;
+            MixedBufs &b = m.bufs[fam][c];
+            const size_t bytes = kTableHeader + sizeof(gmle::GroupDesc) * (size_t)b.h_header[0];
+            CK(cudaMemcpyAsync(b.d_base, b.h_base, bytes, cudaMemcpyHostToDevice, s),
+               "H2D group table");
+            if (record_reuse) CK(cudaEventRecord(b.reuse, s), "cudaEventRecord");
+        }
+    return GMLE_OK;
+}
+
+gmle_status enqueue_plan(gmle_ctx *ctx, MixedSet &m, const MixedPlan &plan, cudaStream_t s)
+{
+    for (const gmle_group &G : plan.plain) {
+        const Tuning t = pick_tuning(ctx, &G.desc, G.n);
+        KernelArgs a = make_args(ctx, &G.desc, G.data, G.x_corners, G.y_corners, G.n, G.params,
+                                 G.crlb, G.llr, G.flags, t.tpr);
+        CK(launch(ctx, &G.desc, a, t.rois_per_block, s), "fit kernel launch");
+    }
+    // The persistent launches of different classes run concurrently (on the
+    // fork streams, joined back into s): small steps of the serving loop
+    // would otherwise leave the GPU idle in each launch's tail.
+    int used = 0;
+    for (int fam = 0; fam < 2; fam++)
+        for (int c = 0; c < kClasses; c++) used += plan.tiles[fam][c] > 0;
+    if (used > 1) CK(cudaEventRecord(m.ev_fork, s), "cudaEventRecord");
+    for (int c = 0; c < kClasses; c++) {
+        cudaStream_t q = s;
+        bool forked = false;
+        for (int fam = 0; fam < 2; fam++) {
+            if (plan.tiles[fam][c] == 0) continue;
+            if (used > 1 && !forked) {
+                q = m.fork[c];
+                CK(cudaStreamWaitEvent(q, m.ev_fork, 0), "cudaStreamWaitEvent");
+                forked = true;
+            }
+            ctx->launches++;
+            gmle_status st = enqueue_mixed(ctx, fam == 1, c, m.bufs[fam][c], plan.smem[fam][c],
+                                           plan.grid[fam][c], q, m.zero_copy);
+            if (st != GMLE_OK) return st;
+        }
+        if (forked) {
+            CK(cudaEventRecord(m.ev_join[c], q), "cudaEventRecord");
+            CK(cudaStreamWaitEvent(s, m.ev_join[c], 0), "cudaStreamWaitEvent");
+        }
     }
     return GMLE_OK;
 }
@@ -745,5 +840,12 @@ extern "C" gmle_status gmle_fit_mixed_device(gmle_ctx *ctx, const gmle_group *gr
     if (ngroups < 0 || (ngroups > 0 && !groups))
         return fail(ctx, GMLE_INVALID_ARG, "groups array is required");
     cudaSetDevice(ctx->device);
-    return run_mixed(ctx, groups, ngroups, (cudaStream_t)stream, ctx->mixed);
+    gmle_status st = init_mixed_set(ctx, ctx->mixed);
+    if (st != GMLE_OK) return st;
+    MixedPlan plan;
+    st = plan_mixed(ctx, groups, ngroups, ctx->mixed, plan, true);
+    if (st != GMLE_OK) return st;
+    st = upload_plan(ctx, ctx->mixed, plan, (cudaStream_t)stream, true);
+    if (st != GMLE_OK) return st;
+    return enqueue_plan(ctx, ctx->mixed, plan, (cudaStream_t)stream);
 }

@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -118,8 +119,8 @@ struct Server {
     cudaStream_t s_step[kMaxSlots] = {};
     cudaEvent_t step_done[kMaxSlots] = {};
     bool slot_busy[kMaxSlots] = {};
-    MixedBufs bufs[kMaxSlots][2];
-    std::map<size_t, cudaGraphExec_t> graphs[kMaxSlots][2];
+    MixedSet sets[kMaxSlots];
+    std::map<std::array<size_t, 2 * kClasses>, cudaGraphExec_t> graphs[kMaxSlots];
     // statistics
     int64_t submitted = 0, completed = 0, rejected = 0, failed = 0, rois_done = 0, steps = 0;
     std::vector<float> lat_ms;
@@ -219,52 +220,56 @@ struct Server {
         return e;
     }
 
-    // One family of one step: table in the slot's pinned buffer, then a graph
-    // replay (captured on first use for this shared-memory size) or a direct
-    // enqueue.
-    gmle_status launch_family(int slot, bool scmos, const std::vector<gmle_group> &groups)
-    {
-        MixedBufs &b = bufs[slot][scmos];
-        gmle_status st = GMLE_OK;
-        std::lock_guard<std::mutex> lk(ctx->mu);
-        const int64_t tiles = build_mixed_table(ctx, groups.data(), (int32_t)groups.size(), scmos,
-                                                b, &st);
-        if (st != GMLE_OK || tiles == 0) return st;
-        const size_t smem = mixed_smem(groups.data(), (int32_t)groups.size(), scmos);
-        const int grid = mixed_grid(ctx, scmos, smem);
-        ctx->launches++;
-        if (!cfg.use_graphs)
-            return enqueue_mixed(ctx, scmos, b, smem, grid, s_step[slot]);
-        auto it = graphs[slot][scmos].find(smem);
-        if (it == graphs[slot][scmos].end()) {
-            cudaGraph_t g = nullptr;
-            cudaGraphExec_t ge = nullptr;
-            GMLE_CK(cudaStreamBeginCapture(s_step[slot], cudaStreamCaptureModeThreadLocal),
-                    "cudaStreamBeginCapture");
-            st = enqueue_mixed(ctx, scmos, b, smem, grid, s_step[slot]);
-            cudaError_t e = cudaStreamEndCapture(s_step[slot], &g);
-            if (st != GMLE_OK) {
-                if (g) cudaGraphDestroy(g);
-                return st;
-            }
-            GMLE_CK(e, "cudaStreamEndCapture");
-            e = cudaGraphInstantiate(&ge, g, 0);
-            cudaGraphDestroy(g);
-            GMLE_CK(e, "cudaGraphInstantiate");
-            it = graphs[slot][scmos].emplace(smem, ge).first;
-        }
-        GMLE_CK(cudaGraphLaunch(it->second, s_step[slot]), "cudaGraphLaunch");
-        return GMLE_OK;
-    }
-
+    // One step: the tables of every (family, class) in the slot's pinned
+    // buffers, then a replay of the slot's graph for this launch pattern
+    // (captured on first use) or a direct enqueue.
     gmle_status launch_step(int slot, const std::vector<Request *> &reqs)
     {
         std::vector<gmle_group> groups;
         groups.reserve(reqs.size());
         for (Request *r : reqs) groups.push_back(r->dev);
-        for (int fam = 0; fam < 2; fam++) {
-            gmle_status st = launch_family(slot, fam == 1, groups);
+        MixedSet &m = sets[slot];
+        MixedPlan plan;
+        {
+            std::lock_guard<std::mutex> lk(ctx->mu);
+            gmle_status st = plan_mixed(ctx, groups.data(), (int32_t)groups.size(), m, plan,
+                                        false);
             if (st != GMLE_OK) return st;
+            // zero-copy tables: nothing to upload; the graph holds the launches
+            st = upload_plan(ctx, m, plan, s_step[slot], false);
+            if (st != GMLE_OK) return st;
+            if (!cfg.use_graphs) {
+                st = enqueue_plan(ctx, m, plan, s_step[slot]);
+                if (st != GMLE_OK) return st;
+            } else {
+                std::array<size_t, 2 * kClasses> key{};
+                for (int f = 0; f < 2; f++)
+                    for (int c = 0; c < kClasses; c++)
+                        key[f * kClasses + c] = plan.tiles[f][c] ? plan.smem[f][c] : 0;
+                auto it = graphs[slot].find(key);
+                if (it == graphs[slot].end()) {
+                    cudaGraph_t g = nullptr;
+                    cudaGraphExec_t ge = nullptr;
+                    GMLE_CK(cudaStreamBeginCapture(s_step[slot], cudaStreamCaptureModeThreadLocal),
+                            "cudaStreamBeginCapture");
+                    st = enqueue_plan(ctx, m, plan, s_step[slot]);
+                    const cudaError_t e = cudaStreamEndCapture(s_step[slot], &g);
+                    if (st != GMLE_OK) {
+                        if (g) cudaGraphDestroy(g);
+                        return st;
+                    }
+                    GMLE_CK(e, "cudaStreamEndCapture");
+                    const cudaError_t e2 = cudaGraphInstantiate(&ge, g, 0);
+                    cudaGraphDestroy(g);
+                    GMLE_CK(e2, "cudaGraphInstantiate");
+                    it = graphs[slot].emplace(key, ge).first;
+                } else {
+                    // a replay launches the same kernels as the capture
+                    for (int f = 0; f < 2; f++)
+                        for (int c = 0; c < kClasses; c++) ctx->launches += plan.tiles[f][c] > 0;
+                }
+                GMLE_CK(cudaGraphLaunch(it->second, s_step[slot]), "cudaGraphLaunch");
+            }
         }
         GMLE_CK(cudaEventRecord(step_done[slot], s_step[slot]), "cudaEventRecord");
         return GMLE_OK;
@@ -409,10 +414,8 @@ void server_destroy(gmle_ctx *ctx)
     cudaSetDevice(ctx->device);
     for (int k = 0; k < kMaxSlots; k++) {
         if (S->s_step[k]) cudaStreamSynchronize(S->s_step[k]);
-        for (int f = 0; f < 2; f++) {
-            for (auto &g : S->graphs[k][f]) cudaGraphExecDestroy(g.second);
-            free_mixed(S->bufs[k][f]);
-        }
+        for (auto &g : S->graphs[k]) cudaGraphExecDestroy(g.second);
+        free_mixed_set(S->sets[k]);
         if (S->s_step[k]) cudaStreamDestroy(S->s_step[k]);
         if (S->step_done[k]) cudaEventDestroy(S->step_done[k]);
     }
@@ -447,7 +450,7 @@ gmle_status gmle_server_start(gmle_ctx *ctx, const gmle_server_config *config)
     } else {
         S->cfg.use_graphs = 1;
     }
-    if (S->cfg.max_inflight_steps <= 0) S->cfg.max_inflight_steps = 2;
+    if (S->cfg.max_inflight_steps <= 0) S->cfg.max_inflight_steps = 4;
     S->cfg.max_inflight_steps = std::min(S->cfg.max_inflight_steps, kMaxSlots);
     if (S->cfg.max_step_rois <= 0) S->cfg.max_step_rois = 1ll << 21;
     if (S->cfg.max_pending <= 0) S->cfg.max_pending = 1 << 16;
@@ -477,12 +480,17 @@ gmle_status gmle_server_start(gmle_ctx *ctx, const gmle_server_config *config)
     for (int k = 0; ok && k < S->cfg.max_inflight_steps; k++) {
         ok = cudaStreamCreateWithFlags(&S->s_step[k], cudaStreamNonBlocking) == cudaSuccess &&
              cudaEventCreateWithFlags(&S->step_done[k], cudaEventDisableTiming) == cudaSuccess;
+        ok = ok && init_mixed_set(ctx, S->sets[k]) == GMLE_OK;
+        S->sets[k].zero_copy = true;
         for (int f = 0; ok && f < 2; f++)
-            ok = ensure_mixed(ctx, S->bufs[k][f], kServerTableCap) == GMLE_OK;
+            for (int c = 0; ok && c < kClasses; c++)
+                ok = ensure_mixed(ctx, S->sets[k].bufs[f][c], kServerTableCap) == GMLE_OK;
     }
     // set the kernels' shared-memory attribute outside any graph capture
-    gmle::mixed_blocks_per_sm(false, 48 * 1024);
-    gmle::mixed_blocks_per_sm(true, 48 * 1024);
+    for (int c = 0; c < kClasses; c++) {
+        gmle::mixed_blocks_per_sm(false, c, 48 * 1024);
+        gmle::mixed_blocks_per_sm(true, c, 48 * 1024);
+    }
     ctx->server = S;
     if (!ok) {
         server_destroy(ctx);

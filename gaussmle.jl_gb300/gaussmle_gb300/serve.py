@@ -54,7 +54,7 @@ class Server:
     """The context's serving loop.  Host buffers passed to submit() must stay
     alive until the request is waited for."""
 
-    def __init__(self, ctx: _lib.Context, hbm_budget_bytes: int = 0, max_inflight_steps: int = 2,
+    def __init__(self, ctx: _lib.Context, hbm_budget_bytes: int = 0, max_inflight_steps: int = 4,
                  max_step_rois: int = 0, max_pending: int = 0, use_graphs: bool = True):
         self.ctx = ctx
         cfg = _lib.ServerConfig(hbm_budget_bytes, max_inflight_steps, max_step_rois,

@@ -339,3 +339,65 @@ def device_workload(model: int, box: int, camera: int, n: int, seed: int = 2024,
         out.update(var=var, gain=gain, offset=off, xc=xc, yc=yc, ny=sensor, nx=sensor)
     out["data"] = e.float().contiguous().view(-1)
     return out
+
+
+def config3_device(n: int = 2_000_000, seed: int = 1003, sensor: int = 2048, device="cuda"):
+    """Workload 3 on the device: a mixed batch of n ROIs in the MIX proportions
+    (40% XYNB 11x11, 25% XYNBS 9x9, 15% XYNBSXSY 13x13 with sigma_x, sigma_y
+    U(1, 2), 15% astigmatic 15x15, 5% XYNB 7x7), N log-uniform 100..20000,
+    bg U(1, 20), sCMOS ADU data on one shared 2048x2048 calibration map set.
+    Returns (maps dict, list of group dicts like device_workload())."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    f64 = dict(dtype=torch.float64, device=device)
+    var = torch.exp(np.log(2.0) + 0.5 * torch.randn((sensor, sensor), generator=g, **f64)).float()
+    gain = (0.4 + 0.2 * torch.rand((sensor, sensor), generator=g, **f64)).float()
+    off = torch.full((sensor, sensor), 100.0, dtype=torch.float32, device=device)
+    maps = {"var": var, "gain": gain, "offset": off, "ny": sensor, "nx": sensor}
+    counts = [int(round(f * n)) for f, _, _ in MIX]
+    counts[0] += n - sum(counts)
+    groups = []
+    for (frac, model, box), cnt in zip(MIX, counts):
+        c = (box + 1) / 2.0
+        u = lambda lo, hi: lo + (hi - lo) * torch.rand(cnt, generator=g, **f64)
+        x, y, bg = u(c - 1.5, c + 1.5), u(c - 1.5, c + 1.5), u(1, 20)
+        N = torch.exp(u(np.log(100.0), np.log(20000.0)))
+        if model == MODEL_XYNB:
+            psf, cons = GaussianXYNB(1.3), default_constraints(GaussianXYNB(1.3), 11)
+            sx = sy = torch.full((cnt,), 1.3, **f64)
+            truth = torch.stack([x, y, N, bg], 1)
+        elif model == MODEL_XYNBS:
+            psf = GaussianXYNBS()
+            cons = default_constraints(psf, 11)
+            sx = sy = u(1.0, 1.8)
+            truth = torch.stack([x, y, N, bg, sx], 1)
+        elif model == MODEL_XYNBSXSY:
+            psf = GaussianXYNBSXSY()
+            cons = default_constraints(psf, 11)
+            sx, sy = u(1.0, 2.0), u(1.0, 2.0)
+            truth = torch.stack([x, y, N, bg, sx, sy], 1)
+        else:
+            psf = AstigmaticXYZNB(1.3, 1.3, 0.05, 0.05, 0.3, 0.3, 50.0, 100.0)
+            cons = ASTIG_WIDE
+            z = u(-400, 400)
+            zx, zy = (z - psf.gamma) / psf.d, (z + psf.gamma) / psf.d
+            sx = psf.sx0 * torch.sqrt(1 + zx ** 2 + psf.Ax * zx ** 3 + psf.Bx * zx ** 4)
+            sy = psf.sy0 * torch.sqrt(1 + zy ** 2 + psf.Ay * zy ** 3 + psf.By * zy ** 4)
+            truth = torch.stack([x, y, z, N, bg], 1)
+        px = _psf_1d_t(torch, x, sx, box)
+        py = _psf_1d_t(torch, y, sy, box)
+        mu = bg[:, None, None] + N[:, None, None] * px[:, :, None] * py[:, None, :]
+        e = torch.poisson(mu, generator=g)
+        xc = torch.randint(1, sensor - box + 2, (cnt,), generator=g, device=device, dtype=torch.int32)
+        yc = torch.randint(1, sensor - box + 2, (cnt,), generator=g, device=device, dtype=torch.int32)
+        jj = torch.arange(box, device=device)[None, :, None]
+        ii = torch.arange(box, device=device)[None, None, :]
+        cols = (xc.long()[:, None, None] - 1) + jj
+        rows = (yc.long()[:, None, None] - 1) + ii
+        e = e + torch.randn(e.shape, generator=g, **f64) * var[cols, rows].double().sqrt()
+        e = e / gain[cols, rows].double() + off[cols, rows].double()
+        groups.append({"data": e.float().contiguous().view(-1), "xc": xc, "yc": yc,
+                       "truth": truth.float(), "box": box, "n": cnt, "psf": psf, "model": model,
+                       "camera": CAMERA_SCMOS_ADU, "constraints": cons})
+    return maps, groups

@@ -216,7 +216,7 @@ gmle_status gmle_fit_mixed_device(gmle_ctx *ctx, const gmle_group *groups, int32
  */
 typedef struct {
     int64_t hbm_budget_bytes;   /* device arena; 0 = half of the free HBM at start */
-    int32_t max_inflight_steps; /* concurrent kernel launches; 0 = 2 */
+    int32_t max_inflight_steps; /* concurrent launch steps; 0 = 4 */
     int64_t max_step_rois;      /* ROIs per launch; 0 = 2^21 */
     int32_t max_pending;        /* queued requests before submit rejects; 0 = 1 << 16 */
     int32_t use_graphs;         /* 1: each launch is a replay of a captured CUDA graph */
