@@ -1,0 +1,139 @@
+"""Statistical acceptance protocols of the reference's test-suite, re-expressed.
+
+They do not compare against another implementation but against simulated
+ground truth, exactly as GaussMLE.jl's own tests do:
+  * model validation: 1000 blobs, 15x15, N = 1000 U(0.8, 1.2), bg = 5 U(0.8, 1.2),
+    sigma = 1.3 (x U(0.8, 1.2) for fitted widths), x, y = box/2 + 0.5 randn;
+    |bias| below per-parameter tolerances and |1 - std/mean(CRLB)| < 0.1
+    (test/validation_utils.jl:68-172, :174-300, :321-350);
+  * sCMOS photometry: uniform 5 e- read noise, gain 0.5, offset 100, qe 0.82,
+    photon bias < 50 e- against N*qe, |1 - std/CRLB| < 0.3, mean CRLB > 30
+    (test/model_validation_tests.jl:208-281);
+  * sCMOS variance-map indexing: variance 1 + 0.5 (row-1) + 0.05 (col-1) on a
+    512x512 map; ROIs at (x, y) corners (400, 50) and (50, 400); the mean x
+    CRLB ratio B / A in (1.5, 3.0) and within 40 % of sqrt(var_B / var_A)
+    (test/model_validation_tests.jl:283-393);
+  * precision improves with photons (test/test_strict_validation.jl:376-430).
+Each protocol takes a `fit(model, box, camera, data, xc, yc, maps, constraints)`
+callable returning (params (n, P), crlb (n, P)), so the oracle and the GPU
+run the same protocol.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from gaussmle_gb300 import simulate
+from gaussmle_gb300.constraints import default_constraints
+from gaussmle_gb300.models import GaussianXYNB, GaussianXYNBS, GaussianXYNBSXSY
+
+# (bias tolerance, std/CRLB tolerance), test/validation_utils.jl:321-330
+TOL = {"x": (0.15, 0.1), "y": (0.15, 0.1), "photons": (100.0, 0.1), "bg": (2.0, 0.1),
+       "sigma": (0.05, 0.1), "sigma_x": (0.05, 0.1), "sigma_y": (0.05, 0.1)}
+
+
+def model_validation_data(model: int, n: int = 1000, box: int = 15, seed: int = 42):
+    rng = np.random.Generator(np.random.Philox(seed))
+    x = box / 2 + 0.5 * rng.standard_normal(n)
+    y = box / 2 + 0.5 * rng.standard_normal(n)
+    N = 1000.0 * rng.uniform(0.8, 1.2, n)
+    bg = 5.0 * rng.uniform(0.8, 1.2, n)
+    if model == 0:
+        psf, truth = GaussianXYNB(1.3), np.stack([x, y, N, bg], 1)
+    elif model == 1:
+        psf, truth = GaussianXYNBS(), np.stack([x, y, N, bg, 1.3 * rng.uniform(0.8, 1.2, n)], 1)
+    else:
+        psf = GaussianXYNBSXSY()
+        truth = np.stack([x, y, N, bg, 1.3 * rng.uniform(0.8, 1.2, n),
+                          1.3 * rng.uniform(0.8, 1.2, n)], 1)
+    truth = truth.astype(np.float32)
+    data = simulate.poisson_rois(rng, psf, truth, box)
+    return psf, truth, data
+
+
+def check_model_validation(fit, model: int, n: int = 1000, box: int = 15) -> dict:
+    psf, truth, data = model_validation_data(model, n, box)
+    cons = default_constraints(psf, 11)   # the reference's fitter default
+    ones = np.ones(n, np.int32)
+    params, crlb = fit(model, box, 0, psf, data, ones, ones, None, cons)
+    out = {}
+    for k, name in enumerate(psf.param_names):
+        err = params[:, k].astype(np.float64) - truth[:, k]
+        bias = float(err.mean())
+        ratio = float(err.std(ddof=1) / crlb[:, k].mean())
+        btol, stol = TOL[name]
+        out[name] = {"bias": bias, "std_ratio": ratio,
+                     "pass": abs(bias) < btol and abs(1 - ratio) < stol}
+    return out
+
+
+def check_scmos_photometry(fit, n: int = 500, box: int = 15) -> dict:
+    from gaussmle_gb300.camera import SCMOSCamera
+    rng = np.random.Generator(np.random.Philox(42))
+    cam = SCMOSCamera(512, 512, 0.1, readnoise=np.full((512, 512), 5.0, np.float32),
+                      offset=100.0, gain=0.5, qe=0.82)
+    psf = GaussianXYNB(1.3)
+    truth = np.stack([box / 2 + 0.5 * rng.standard_normal(n),
+                      box / 2 + 0.5 * rng.standard_normal(n),
+                      1000 + 200 * rng.standard_normal(n),
+                      10 + 2 * rng.standard_normal(n)], 1).astype(np.float32)
+    per_row = (512 - box + 1) // box
+    k = np.arange(n)
+    xc = (1 + (k % per_row) * box).astype(np.int32)
+    yc = (1 + (k // per_row) * box).astype(np.int32)
+    maps = cam.calibration_maps()
+    # photons -> e- with qe, readout noise, ADU (src/simulator.jl:281-307)
+    data = simulate.scmos_rois(rng, psf, truth, box, maps, xc, yc, qe=0.82)
+    params, crlb = fit(0, box, 2, psf, data, xc, yc, maps, default_constraints(psf, 11))
+    err = params[:, 2].astype(np.float64) - truth[:, 2] * 0.82
+    bias = float(err.mean())
+    ratio = float(err.std(ddof=1) / crlb[:, 2].mean())
+    return {"bias": bias, "std_ratio": ratio, "mean_crlb": float(crlb[:, 2].mean()),
+            "pass": abs(bias) < 50 and abs(1 - ratio) < 0.3 and crlb[:, 2].mean() > 30}
+
+
+def check_variance_indexing(fit, box: int = 15) -> dict:
+    rng = np.random.Generator(np.random.Philox(123))
+    size = 512
+    i = np.arange(size)[:, None]
+    j = np.arange(size)[None, :]
+    var = (1.0 + 0.5 * i + 0.05 * j).astype(np.float32)       # map[row = y, col = x]
+    gain = np.ones_like(var)
+    off = np.zeros_like(var)
+    npg = 50
+    n = 2 * npg
+    truth = np.stack([box / 2 + 0.3 * rng.standard_normal(n),
+                      box / 2 + 0.3 * rng.standard_normal(n),
+                      np.full(n, 2000.0), np.full(n, 5.0)], 1).astype(np.float32)
+    xc = np.array([400] * npg + [50] * npg, np.int32)
+    yc = np.array([50] * npg + [400] * npg, np.int32)
+    psf = GaussianXYNB(1.3)
+    data = simulate.scmos_rois(rng, psf, truth, box, (var, gain, off), xc, yc)
+    params, crlb = fit(0, box, 2, psf, data, xc, yc, (var, gain, off),
+                       default_constraints(psf, 11))
+    a, b = crlb[:npg, 0].mean(), crlb[npg:, 0].mean()
+    c = box // 2
+    var_a = 1 + 0.5 * (50 + c - 1) + 0.05 * (400 + c - 1)
+    var_b = 1 + 0.5 * (400 + c - 1) + 0.05 * (50 + c - 1)
+    expected = float(np.sqrt(var_b / var_a))
+    ratio = float(b / a)
+    return {"ratio": ratio, "expected": expected,
+            "pass": 1.5 < ratio < 3.0 and abs(ratio - expected) / expected < 0.4}
+
+
+def check_precision_vs_photons(fit, box: int = 11) -> dict:
+    psf = GaussianXYNB(1.3)
+    cons = default_constraints(psf, 11)
+    out = []
+    for k, N in enumerate([500.0, 2000.0, 8000.0]):
+        rng = np.random.Generator(np.random.Philox(1000 + k))
+        n = 400
+        truth = np.stack([box / 2 + 0.5 * rng.standard_normal(n),
+                          box / 2 + 0.5 * rng.standard_normal(n),
+                          np.full(n, N), np.full(n, 10.0)], 1).astype(np.float32)
+        data = simulate.poisson_rois(rng, psf, truth, box)
+        ones = np.ones(n, np.int32)
+        params, crlb = fit(0, box, 0, psf, data, ones, ones, None, cons)
+        out.append((N, float(np.std(params[:, 0] - truth[:, 0])), float(crlb[:, 0].mean())))
+    stds = [o[1] for o in out]
+    crlbs = [o[2] for o in out]
+    return {"rows": out, "pass": stds[0] > stds[1] > stds[2] and crlbs[0] > crlbs[1] > crlbs[2]}

@@ -1,0 +1,104 @@
+"""CPU checks of the oracle (the checker of the CUDA path).
+
+* Its CRLB code agrees with the reference's own first-principles Fisher /
+  CRLB derivation (dev/astig_theory/compute_theoretical_crlb.jl, restated in
+  tests/golden/make_golden.py).
+* It reproduces its committed golden fixtures.
+* It passes the reference test-suite's statistical acceptance protocols
+  (tests/statistics_cases.py).
+* FP32 and FP64 builds agree for well-conditioned fits.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import statistics_cases as SC
+from oracle import oracle as O
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def oracle_fit(model, box, camera, psf, data, xc, yc, maps, cons, precision="f32"):
+    d = O.make_desc(model, box, 20, camera, psf.psf_vector(), cons.lower, cons.upper,
+                    cons.max_step)
+    r = O.fit(d, data, xc, yc, maps, precision)
+    return r["params"], r["crlb"]
+
+
+@pytest.mark.parametrize("precision,rtol", [("f64", 1e-6), ("f32", 2e-3)])
+def test_crlb_matches_reference_theory_derivation(precision, rtol):
+    g = np.load(GOLDEN / "astig_theory_crlb.npz")
+    for th, ref in zip(g["theta"], g["crlb"]):
+        got, flags = O.crlb_at(3, int(g["box"]), g["psf"], th, precision)
+        assert flags & O.FLAG_CONVERGED
+        np.testing.assert_allclose(got, ref, rtol=rtol)
+
+
+@pytest.mark.parametrize("path", sorted(GOLDEN.glob("oracle_*.npz")), ids=lambda p: p.stem)
+def test_oracle_reproduces_golden_fixture(path):
+    g = np.load(path)
+    maps = (g["var"], g["gain"], g["offset"]) if int(g["camera"]) else None
+    d = O.make_desc(int(g["model"]), int(g["box"]), 20, int(g["camera"]), g["psf"], g["lower"],
+                    g["upper"], g["max_step"])
+    r = O.fit(d, g["data"], g["xc"], g["yc"], maps, "f32")
+    np.testing.assert_allclose(r["params"], g["params"], rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(r["crlb"], g["crlb"], rtol=1e-5)
+    np.testing.assert_allclose(r["llr"], g["llr"], rtol=1e-5, atol=1e-5)
+    assert np.array_equal(r["flags"], g["flags"])
+
+
+@pytest.mark.parametrize("model", [0, 1, 2], ids=["xynb", "xynbs", "xynbsxsy"])
+def test_model_validation_protocol(model):
+    res = SC.check_model_validation(oracle_fit, model)
+    assert all(v["pass"] for v in res.values()), res
+
+
+def test_scmos_photometry_protocol():
+    res = SC.check_scmos_photometry(oracle_fit)
+    assert res["pass"], res
+
+
+def test_scmos_variance_map_indexing_protocol():
+    res = SC.check_variance_indexing(oracle_fit)
+    assert res["pass"], res
+
+
+def test_precision_improves_with_photons():
+    res = SC.check_precision_vs_photons(oracle_fit)
+    assert res["pass"], res
+
+
+def test_fp32_and_fp64_builds_agree_when_well_conditioned():
+    psf, truth, data = SC.model_validation_data(0, n=300, box=11, seed=9)
+    from gaussmle_gb300.constraints import default_constraints
+    cons = default_constraints(psf, 11)
+    ones = np.ones(300, np.int32)
+    p32, c32 = oracle_fit(0, 11, 0, psf, data, ones, ones, None, cons, "f32")
+    p64, c64 = oracle_fit(0, 11, 0, psf, data, ones, ones, None, cons, "f64")
+    assert np.abs(p32[:, :2] - p64[:, :2]).max() < 1e-4
+    np.testing.assert_allclose(c32, c64, rtol=1e-4)
+
+
+def test_oracle_rejects_bad_descriptors():
+    d = O.make_desc(7, 11, 20, 0, np.zeros(8), [0] * 4, [1] * 4, [1] * 4)
+    with pytest.raises(ValueError):
+        O.fit(d, np.zeros((11, 11, 1), np.float32))
+    d = O.make_desc(0, 2, 20, 0, np.zeros(8), [0] * 4, [1] * 4, [1] * 4)
+    with pytest.raises(ValueError):
+        O.fit(d, np.zeros((2, 2, 1), np.float32))
+
+
+def test_zero_iterations_returns_the_initial_estimate():
+    psf, truth, data = SC.model_validation_data(0, n=10, box=11, seed=3)
+    from gaussmle_gb300.constraints import default_constraints
+    c = default_constraints(psf, 11)
+    d = O.make_desc(0, 11, 0, 0, psf.psf_vector(), c.lower, c.upper, c.max_step)
+    r = O.fit(d, data)
+    # the reference initialisation (src/unified_kernel.jl:158-192): bg = mean of
+    # the edge pixels, photons = max(sum(max(0, d - bg)), 100)
+    roi = np.asarray(data[:, :, 0], np.float64)
+    edge = np.concatenate([roi[0, :], roi[-1, :], roi[1:-1, 0], roi[1:-1, -1]])
+    assert abs(r["params"][0, 3] - edge.mean()) < 1e-3
+    sig = np.maximum(0, roi - edge.mean()).sum()
+    assert abs(r["params"][0, 2] - max(sig, 100)) / max(sig, 100) < 1e-5
