@@ -1,0 +1,124 @@
+"""
+    GaussMLEGB300
+
+`ccall` binding of libgaussmle_sm100a.so (include/gaussmle_gb300.h) for
+GaussMLE.jl.  It replaces the GPU branches of `fit` (src/interface.jl:217-263,
+:334-370, :421-457): everything before them (validation, `to_pixel_units`,
+corners) and after them (p-values, `create_localization_result`, `to_smld`)
+stays in GaussMLE, so `fit` still returns the same `BasicSMLD` emitters.
+
+There is no CPU fallback: `Context()` throws when the library or an sm_103a
+GPU is missing.
+"""
+module GaussMLEGB300
+
+using GaussMLE: GaussMLE, PSFModel, GaussianXYNB, GaussianXYNBS, GaussianXYNBSXSY,
+                AstigmaticXYZNB, ParameterConstraints
+
+const libgmle = get(ENV, "GAUSSMLE_GB300_LIB",
+                    joinpath(@__DIR__, "..", "lib", "libgaussmle_sm100a.so"))
+
+const CAMERA_POISSON = Int32(0)
+const CAMERA_SCMOS = Int32(1)
+const CAMERA_SCMOS_ADU = Int32(2)
+
+# gmle_fit_desc
+struct FitDesc
+    model::Int32
+    box::Int32
+    iterations::Int32
+    camera::Int32
+    psf::NTuple{8,Float32}
+    lower::NTuple{6,Float32}
+    upper::NTuple{6,Float32}
+    max_step::NTuple{6,Float32}
+end
+
+model_id(::GaussianXYNB) = Int32(0)
+model_id(::GaussianXYNBS) = Int32(1)
+model_id(::GaussianXYNBSXSY) = Int32(2)
+model_id(::AstigmaticXYZNB) = Int32(3)
+
+psf_vector(p::GaussianXYNB) = (Float32(p.σ), 0f0, 0f0, 0f0, 0f0, 0f0, 0f0, 0f0)
+psf_vector(::GaussianXYNBS) = ntuple(_ -> 0f0, 8)
+psf_vector(::GaussianXYNBSXSY) = ntuple(_ -> 0f0, 8)
+psf_vector(p::AstigmaticXYZNB) = Float32.((p.σx₀, p.σy₀, p.Ax, p.Ay, p.Bx, p.By, p.γ, p.d))
+
+pad6(v) = ntuple(k -> k <= length(v) ? Float32(v[k]) : 0f0, 6)
+
+function FitDesc(psf_pixels::PSFModel, box::Integer, iterations::Integer, camera::Integer,
+                 c::ParameterConstraints)
+    FitDesc(model_id(psf_pixels), Int32(box), Int32(iterations), Int32(camera),
+            psf_vector(psf_pixels), pad6(c.lower), pad6(c.upper), pad6(c.max_step))
+end
+
+mutable struct Context
+    ptr::Ptr{Cvoid}
+end
+
+function Context(device::Integer = 0)
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    st = ccall((:gmle_create, libgmle), Cint, (Ref{Ptr{Cvoid}}, Cint), r, device)
+    st == 0 || error("GaussMLEGB300: no usable GB300 on device $device (status $st); " *
+                     "this backend has no CPU fallback")
+    ctx = Context(r[])
+    finalizer(c -> ccall((:gmle_destroy, libgmle), Cvoid, (Ptr{Cvoid},), c.ptr), ctx)
+    return ctx
+end
+
+function check(ctx::Context, st::Cint)
+    st == 0 && return nothing
+    msg = unsafe_string(ccall((:gmle_last_error, libgmle), Cstring, (Ptr{Cvoid},), ctx.ptr))
+    error("GaussMLEGB300 (status $st): $msg")
+end
+
+const DEFAULT_CONTEXT = Ref{Union{Nothing,Context}}(nothing)
+default_context() = something(DEFAULT_CONTEXT[], (DEFAULT_CONTEXT[] = Context(0)))
+
+"""
+    set_calibration!(ctx, variance, gain=nothing, offset=nothing)
+
+Upload full-sensor (ny, nx) maps once; they stay resident on the GPU
+(replaces the per-batch variance-map copy of src/interface.jl:431-432).
+"""
+function set_calibration!(ctx::Context, variance::AbstractMatrix, gain = nothing,
+                          offset = nothing)
+    v = Matrix{Float32}(variance)
+    g = gain === nothing ? C_NULL : Matrix{Float32}(gain)
+    o = offset === nothing ? C_NULL : Matrix{Float32}(offset)
+    GC.@preserve v g o begin
+        st = ccall((:gmle_set_calibration, libgmle), Cint,
+                   (Ptr{Cvoid}, Ptr{Float32}, Ptr{Float32}, Ptr{Float32}, Int32, Int32),
+                   ctx.ptr, v, g, o, size(v, 1), size(v, 2))
+    end
+    check(ctx, st)
+end
+
+"""
+    fit!(results, uncertainties, log_likelihoods, data, psf_pixels, camera,
+         x_corners, y_corners, constraints, iterations; ctx)
+
+The GPU branch of `fit`: `data` is (box, box, n) Float32, `results` and
+`uncertainties` (P, n), `log_likelihoods` (n) - the arrays GaussMLE already
+allocates (src/interface.jl:195-197).  Returns the per-ROI flags.
+"""
+function fit!(results::Matrix{Float32}, uncertainties::Matrix{Float32},
+              log_likelihoods::Vector{Float32}, data::Array{Float32,3}, psf_pixels::PSFModel,
+              camera::Integer, x_corners::Vector{Int32}, y_corners::Vector{Int32},
+              constraints::ParameterConstraints, iterations::Integer;
+              ctx::Context = default_context())
+    box, n = size(data, 1), size(data, 3)
+    desc = Ref(FitDesc(psf_pixels, box, iterations, camera, constraints))
+    flags = Vector{UInt8}(undef, n)
+    GC.@preserve data x_corners y_corners results uncertainties log_likelihoods flags begin
+        st = ccall((:gmle_fit, libgmle), Cint,
+                   (Ptr{Cvoid}, Ref{FitDesc}, Ptr{Float32}, Ptr{Int32}, Ptr{Int32}, Int64,
+                    Ptr{Float32}, Ptr{Float32}, Ptr{Float32}, Ptr{UInt8}),
+                   ctx.ptr, desc, data, x_corners, y_corners, n, results, uncertainties,
+                   log_likelihoods, flags)
+    end
+    check(ctx, st)
+    return flags
+end
+
+end # module
