@@ -45,7 +45,7 @@ struct Slot {
 
 // Group table of one mixed-batch launch: header {groups, tiles} and group
 // descriptors, built in pinned host memory and copied to the device before
-// the launch (one copy of 64 + 224 * groups bytes); and the device
+// the launch (one copy of 64 + 192 * groups bytes); and the device
 // work-stealing tile counter.
 constexpr size_t kTableHeader = 64;
 struct MixedBufs {

@@ -143,6 +143,10 @@ cudaError_t launch_mixed_poisson(int cls, const MixedArgs &m, size_t smem, int g
 cudaError_t launch_mixed_scmos(int cls, const MixedArgs &m, size_t smem, int grid, cudaStream_t s);
 int mixed_blocks_per_sm_poisson(int cls, size_t smem);
 int mixed_blocks_per_sm_scmos(int cls, size_t smem);
+// Set the dynamic shared-memory limit of the family's three kernels on the
+// current device (a per-device set-up step of the no-allocation entry point).
+cudaError_t mixed_set_attributes_poisson();
+cudaError_t mixed_set_attributes_scmos();
 
 inline cudaError_t launch_mixed(bool scmos, int cls, const MixedArgs &m, size_t smem, int grid,
                                 cudaStream_t s)

@@ -45,4 +45,14 @@ int mixed_blocks_per_sm_poisson(int cls, size_t smem)
     return nb;
 }
 
+cudaError_t mixed_set_attributes_poisson()
+{
+    for (int c = 0; c < 3; c++) {
+        cudaError_t e = cudaFuncSetAttribute(kernel_of(c), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             kMixedMaxSmem);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 }  // namespace gmle

@@ -34,7 +34,7 @@ EXPORTED = [
     "gmle_set_calibration", "gmle_fit", "gmle_fit_device", "gmle_fit_device_errors",
     "gmle_get_tuning", "gmle_set_tuning", "gmle_autotune", "gmle_kernel_launches",
     "gmle_fit_mixed_device", "gmle_server_start", "gmle_server_stop", "gmle_submit",
-    "gmle_poll", "gmle_wait", "gmle_server_stats_get",
+    "gmle_poll", "gmle_wait", "gmle_server_stats_get", "gmle_fit_mixed_device_noalloc",
 ]
 
 
@@ -128,6 +128,8 @@ def load(path: str | Path | None = None) -> C.CDLL:
             "gmle_poll": ([vp, C.c_uint64], C.c_int),
             "gmle_wait": ([vp, C.c_uint64, i64], C.c_int),
             "gmle_server_stats_get": ([vp, C.POINTER(ServerStats), i32], C.c_int),
+            "gmle_fit_mixed_device_noalloc": ([C.POINTER(Group), i32, vp, vp, vp, i32, i32, vp,
+                                               C.c_char_p, i32], C.c_int),
         }
         for name, (args, res) in sigs.items():
             f = getattr(lib, name)

@@ -25,7 +25,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2",
               f"-I{REPO_ROOT / 'include'}"]
 SOURCES = ["gmle_fit_xynb.cu", "gmle_fit_xynbs.cu", "gmle_fit_xynbsxsy.cu",
            "gmle_fit_astig.cu", "gmle_mixed_poisson.cu", "gmle_mixed_scmos.cu",
-           "gmle_runtime.cu", "gmle_server.cu"]
+           "gmle_runtime.cu", "gmle_server.cu", "gmle_noalloc.cu"]
 
 
 def nvcc() -> str:

@@ -204,6 +204,49 @@ gmle_status gmle_fit_mixed_device(gmle_ctx *ctx, const gmle_group *groups, int32
                                   void *stream);
 
 /*
+ * gmle_fit_mixed_device for callers that cannot allocate device memory.  No
+ * counterpart in the reference, which allocates its device arrays in every
+ * fit() call (src/interface.jl:229-240, :341-349, :428-436).
+ *
+ * The call allocates nothing: no cudaMalloc, cudaFree, pinned memory, stream,
+ * event or host heap, and it needs no context.  Its scratch is a static device
+ * array of GMLE_NOALLOC_SCRATCH_BYTES (197,120 bytes).  The array holds the
+ * persistent kernels' group tables, their work-stealing tile counters and a
+ * skipped-ROI counter.  It is reserved on each GPU that loads the library's
+ * device code and stays there until the process exits.
+ *
+ * groups    Device pointers, as for gmle_fit_mixed_device.  At most
+ *           GMLE_NOALLOC_MAX_GROUPS groups; a larger ngroups returns
+ *           GMLE_INVALID_ARG and launches nothing.  Every group runs in the
+ *           persistent kernels, including groups of 65536 ROIs or more.
+ * variance, gain, offset
+ *           Device (ny, nx) column-major calibration maps.  NULL when the
+ *           batch is Poisson-only; gain and offset are needed for
+ *           GMLE_CAMERA_SCMOS_ADU.
+ * stream    Must belong to the current device, which the call runs on; used
+ *           as given.
+ * err       May be NULL.  Receives a failure's message, up to err_len bytes.
+ *
+ * Set-up: the first call on a device looks up the scratch address
+ * (cudaGetSymbolAddress) and sets the kernels' attributes.  Make that first
+ * call before any stream capture.
+ *
+ * Zeroing: the tile counters must be zero when each launch starts.  Every
+ * call copies its tables into the scratch with one host-to-device copy on
+ * `stream`, ahead of its launches, and that copy writes the counters to zero.
+ *
+ * Overlap: all calls on a device share the one scratch.  Calls whose GPU work
+ * overlaps race and give undefined results, e.g. calls on different streams
+ * with no event ordering them.  Calls on one stream run in order.
+ */
+#define GMLE_NOALLOC_MAX_GROUPS 1024
+#define GMLE_NOALLOC_SCRATCH_BYTES (512 + 192 * GMLE_NOALLOC_MAX_GROUPS)
+gmle_status gmle_fit_mixed_device_noalloc(const gmle_group *groups, int32_t ngroups,
+                                          const float *variance, const float *gain,
+                                          const float *offset, int32_t ny, int32_t nx,
+                                          void *stream, char *err, int32_t err_len);
+
+/*
  * Serving loop (no reference counterpart: GaussMLE.fit is one blocking call
  * per batch, src/interface.jl:220-262).  A scheduler thread owned by the
  * context admits submitted requests into a device arena (admission by HBM
