@@ -51,6 +51,21 @@ struct KernelArgs {
     unsigned long long *bad_corners;  // device counter of rejected ROIs
 };
 
+// Group table of a table launch.  A table launch fits every group of one
+// (PSF model, box size, camera family) of a mixed batch: its groups' ROIs are
+// cut into tiles of rois_per_block ROIs, numbered group after group, and a
+// persistent grid takes tiles from `counter` (work stealing) until none is
+// left.  With `tiles`, entry t is (group << 32) | (tile index within the
+// group); without it, the tile's group is found by binary search of `tile0`
+// (first tile of each group, increasing).
+struct TileTable {
+    const int64_t *header;        // [0] groups, [1] tiles; nullptr: plain launch
+    const KernelArgs *groups;     // per group: its kernel arguments
+    const int64_t *tiles;         // per tile: (group << 32) | local tile, or nullptr
+    const int64_t *tile0;         // per group: first tile (used when tiles is nullptr)
+    unsigned long long *counter;  // next tile; zero when the launch starts
+};
+
 template <int MODEL> struct ModelInfo;
 template <> struct ModelInfo<0> { static constexpr int P = 4; static constexpr bool SIG = false; };
 template <> struct ModelInfo<1> { static constexpr int P = 5; static constexpr bool SIG = true; };
@@ -421,12 +436,85 @@ __device__ uint8_t crlb_from_fisher(double (&F)[P][P], float *crlb)
 // float2 (data in e-, read-noise variance) for sCMOS), for sCMOS the map
 // offset of each ROI's first pixel (int64), one ok flag per slot, and, when
 // several lanes share a ROI (tpr > 1), NT * BOX y-axis table entries.
-inline size_t smem_bytes(int model, int box, bool scmos, int tpr, int rois)
+__host__ __device__ inline size_t smem_bytes(int model, int box, bool scmos, int tpr, int rois)
 {
     const int nt = model == 0 ? 3 : 5;
     return (size_t)rois * (sizeof(float) * ((size_t)box * box * (scmos ? 2 : 1) +
                                             (tpr > 1 ? (size_t)nt * box : 0)) +
                            (scmos ? sizeof(long long) : 0) + sizeof(int));
+}
+
+// A table launch's block keeps, after the ROI slots, its current group's
+// kernel arguments and the tile it works on.
+struct TableSlot {
+    KernelArgs a;
+    long long tile;  // local tile index within the group; -1: no tile left
+    int grp;         // group whose arguments `a` holds; -1: none yet
+    int next;        // group of the tile just taken
+};
+__host__ __device__ inline size_t table_slot_offset(size_t smem) { return (smem + 15) & ~size_t(15); }
+__host__ __device__ inline size_t table_smem_bytes(size_t smem)
+{
+    return table_slot_offset(smem) + sizeof(TableSlot);
+}
+
+__device__ __forceinline__ TableSlot *table_slot(float *smem, size_t smem_rois)
+{
+    return reinterpret_cast<TableSlot *>(reinterpret_cast<char *>(smem) +
+                                         table_slot_offset(smem_rois));
+}
+
+__device__ __forceinline__ void table_slot_init(TableSlot *ts)
+{
+    if (threadIdx.x == 0) ts->grp = -1;
+}
+
+// The block's next tile of a table launch: thread 0 takes it from the counter
+// and finds its group; when the group changes, the block copies the group's
+// arguments into the slot.  Returns false when no tile is left.  Ends with a
+// barrier, so the slot is stable for the whole tile; the caller puts a
+// barrier between the end of a tile and the next call.
+__device__ __forceinline__ bool table_next(const TileTable &t, int R, TableSlot *ts,
+                                           int64_t &roi0, int &nroi)
+{
+    if (threadIdx.x == 0) {
+        const long long tile = (long long)atomicAdd(t.counter, 1ull);
+        int g = -1;
+        long long local = -1;
+        if (tile < t.header[1]) {
+            if (t.tiles) {
+                const int64_t e = t.tiles[tile];
+                g = (int)(e >> 32);
+                local = e & 0xffffffffLL;
+            } else {
+                // tiles are taken in increasing order: search from the block's group on
+                int lo = ts->grp < 0 ? 0 : ts->grp, hi = (int)t.header[0] - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (t.tile0[mid] <= tile) lo = mid; else hi = mid - 1;
+                }
+                g = lo;
+                local = tile - t.tile0[g];
+            }
+        }
+        ts->tile = local;
+        ts->next = g;
+    }
+    __syncthreads();
+    const int g = ts->next;
+    if (g < 0) return false;
+    if (g != ts->grp) {
+        const int *src = reinterpret_cast<const int *>(t.groups + g);
+        int *dst = reinterpret_cast<int *>(&ts->a);
+        for (int w = threadIdx.x; w < (int)(sizeof(KernelArgs) / sizeof(int)); w += blockDim.x)
+            dst[w] = src[w];
+        __syncthreads();  // the copy is complete and every thread has compared ts->grp
+        if (threadIdx.x == 0) ts->grp = g;
+    }
+    roi0 = ts->tile * R;
+    const int64_t left = ts->a.n - roi0;
+    nroi = left < R ? (int)left : R;
+    return true;
 }
 
 // Asynchronous global -> shared copies (cp.async, sm_80+ PTX); src_bytes = 0
@@ -874,14 +962,30 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
     }
 }
 
-template <int MODEL, int BOX, bool SCMOS>
-__global__ void __launch_bounds__(64) fit_kernel_r1(const KernelArgs a)
+// TABLE = false: plain launch, block b fits ROIs [b R, b R + R) of `a` (the
+// kernel parameter, read from the constant bank).  TABLE = true: table launch
+// (`a` supplies only tpr); the block fits tiles of the table's groups, each
+// through the block's shared-memory copy of the tile's group arguments, until
+// none is left.
+template <int MODEL, int BOX, bool SCMOS, bool TABLE>
+__global__ void __launch_bounds__(64) fit_kernel_r1(const KernelArgs a, const TileTable t)
 {
     extern __shared__ __align__(16) float smem[];
     const int R = blockDim.x;
-    const int64_t roi0 = (int64_t)blockIdx.x * R;
-    const int64_t left = a.n - roi0;
-    fit_rois_r1<MODEL, BOX, SCMOS>(a, roi0, left < R ? (int)left : R, smem);
+    if (!TABLE) {
+        const int64_t roi0 = (int64_t)blockIdx.x * R;
+        const int64_t left = a.n - roi0;
+        fit_rois_r1<MODEL, BOX, SCMOS>(a, roi0, left < R ? (int)left : R, smem);
+        return;
+    }
+    TableSlot *ts = table_slot(smem, smem_bytes(MODEL, BOX, SCMOS, 1, R));
+    table_slot_init(ts);
+    int64_t roi0;
+    int nroi;
+    while (table_next(t, R, ts, roi0, nroi)) {
+        fit_rois_r1<MODEL, BOX, SCMOS>(ts->a, roi0, nroi, smem);
+        __syncthreads();  // the tile's shared memory and slot are free again
+    }
 }
 
 // ---- kernel 2: several threads per ROI ------------------------------------------
@@ -890,8 +994,11 @@ __global__ void __launch_bounds__(64) fit_kernel_r1(const KernelArgs a)
 // block of pixel columns and of y-table rows; the group shares the y tables
 // through shared memory and combines its partial sums with warp shuffles.
 // Used for batches too small to fill the GPU with one thread per ROI.
+//
+// fit_rois_tpr fits ROIs [roi0, roi0 + nroi) of `a` (nroi <= blockDim.x / tpr).
 template <int MODEL, int BOX, bool SCMOS>
-__global__ void __launch_bounds__(256) fit_kernel(const KernelArgs a)
+__device__ __forceinline__ void fit_rois_tpr(const KernelArgs &a, int64_t roi0, int nroi,
+                                             float *smem)
 {
     constexpr int P = ModelInfo<MODEL>::P;
     constexpr bool SIG = ModelInfo<MODEL>::SIG;
@@ -902,15 +1009,11 @@ __global__ void __launch_bounds__(256) fit_kernel(const KernelArgs a)
     constexpr int NB = SIG ? 4 : 3;
     using S = Slots<MODEL>;
 
-    extern __shared__ __align__(16) float smem[];
     const int tpr = a.tpr;
     const int R = blockDim.x / tpr;
     float *spix = smem;
     int *sok = reinterpret_cast<int *>(spix + R * B2 * PS + (SCMOS ? 2 * R : 0));
     float *sytab = reinterpret_cast<float *>(sok + R);
-    const int64_t roi0 = (int64_t)blockIdx.x * R;
-    const int64_t left = a.n - roi0;
-    const int nroi = left < R ? (int)left : R;
     stage_block<BOX, SCMOS>(a, spix, sok, R, roi0, nroi);
 
     const int g = threadIdx.x / tpr;  // ROI slot in the block
@@ -1060,6 +1163,27 @@ __global__ void __launch_bounds__(256) fit_kernel(const KernelArgs a)
                 }
             if (r == 0 && g < nroi) write_result<P>(a, roi0 + g, valid, th, Fm, llr);
         }
+    }
+}
+
+template <int MODEL, int BOX, bool SCMOS, bool TABLE>
+__global__ void __launch_bounds__(256) fit_kernel(const KernelArgs a, const TileTable t)
+{
+    extern __shared__ __align__(16) float smem[];
+    const int R = blockDim.x / a.tpr;
+    if (!TABLE) {
+        const int64_t roi0 = (int64_t)blockIdx.x * R;
+        const int64_t left = a.n - roi0;
+        fit_rois_tpr<MODEL, BOX, SCMOS>(a, roi0, left < R ? (int)left : R, smem);
+        return;
+    }
+    TableSlot *ts = table_slot(smem, smem_bytes(MODEL, BOX, SCMOS, a.tpr, R));
+    table_slot_init(ts);
+    int64_t roi0;
+    int nroi;
+    while (table_next(t, R, ts, roi0, nroi)) {
+        fit_rois_tpr<MODEL, BOX, SCMOS>(ts->a, roi0, nroi, smem);
+        __syncthreads();  // the tile's shared memory and slot are free again
     }
 }
 

@@ -12,7 +12,6 @@
 
 #include "../../include/gaussmle_gb300.h"
 #include "gmle_launch.cuh"
-#include "gmle_mixed.cuh"
 
 namespace gmle_rt {
 
@@ -43,53 +42,68 @@ struct Slot {
     int pend_p = 0;
 };
 
-// Group table of one mixed-batch launch: header {groups, tiles} and group
-// descriptors, built in pinned host memory and copied to the device before
-// the launch (one copy of 64 + 192 * groups bytes); and the device
-// work-stealing tile counter.
-constexpr size_t kTableHeader = 64;
-struct MixedBufs {
-    char *h_base = nullptr, *d_base = nullptr;
-    gmle::GroupDesc *h_groups = nullptr, *d_groups = nullptr;
-    int64_t *h_header = nullptr, *d_header = nullptr;
-    unsigned long long *d_counter = nullptr;
-    int cap = 0;
-    cudaEvent_t reuse = nullptr;  // the last H2D of this table has completed
-};
+// Launch kinds of a mixed batch: one table launch per (camera family, PSF
+// model, box size) present.
+constexpr int kKinds = 2 * 4 * gmle::kNumBoxes;
+inline int kind_of(const gmle_fit_desc &d)
+{
+    return ((d.camera != GMLE_CAMERA_POISSON) * 4 + d.model) * gmle::kNumBoxes +
+           gmle::box_index(d.box);
+}
 
-// Shared-memory classes of the mixed kernel: ROIs up to 9x9, 11x11, 13x13 and
-// up.  Each class present gets its own persistent launch, sized for its
-// largest box, so that small ROIs keep their occupancy.
-constexpr int kClasses = 3;
-using gmle::box_class;
-using gmle::class_tile;
+// Group table of one table launch (gmle::TileTable), built in pinned host
+// memory at fixed offsets:
+//   [0, 64)              header {groups, tiles}
+//   [64, +cap_groups)    per group its KernelArgs
+//   [tiles_off, +cap_tiles)  per tile (group << 32) | local tile
+// The kernels read it in place (zero copy) or from its device copy.
+constexpr size_t kTableHeader = 64;
+struct TableBufs {
+    char *h_base = nullptr, *d_base = nullptr;
+    int64_t cap_groups = 0, cap_tiles = 0;
+    unsigned long long *d_counter = nullptr;
+    cudaEvent_t reuse = nullptr;  // the last copy reading h_base has completed
+    cudaEvent_t used = nullptr;   // the last launch reading d_base has completed
+    size_t tiles_off() const
+    {
+        return kTableHeader + sizeof(gmle::KernelArgs) * (size_t)cap_groups;
+    }
+    size_t bytes() const { return tiles_off() + sizeof(int64_t) * (size_t)cap_tiles; }
+};
 
 // Group tables, fork streams and events of one mixed-batch submitter (the
 // context's synchronous path, or one slot of the serving loop).
+constexpr int kForks = 4;
 struct MixedSet {
-    MixedBufs bufs[2][kClasses];  // [camera family][class]
+    TableBufs tables[kKinds];
     // The kernels read the tables from pinned host memory (no copy).  The
     // serving loop does so: a table copy would queue on the copy engine
     // behind the inputs of every admitted request.
     bool zero_copy = false;
-    cudaStream_t fork[kClasses] = {};
+    cudaStream_t fork[kForks] = {};
     cudaEvent_t ev_fork = nullptr;
-    cudaEvent_t ev_join[kClasses] = {};
+    cudaEvent_t ev_join[kForks] = {};
 };
 
-// What one mixed submission launches: per (family, class), tiles, shared
-// memory and grid; the graph key of the serving loop is the smem vector.
+// One table launch of a plan.
+struct TableLaunch {
+    int kind = -1, model = 0, box = 0;
+    bool scmos = false;
+    gmle::LaunchShape shape{};
+    int64_t groups = 0, tiles = 0;
+};
+
+// What one mixed submission launches: plain launches of large groups, then
+// one table launch per kind present.
 struct MixedPlan {
-    int64_t tiles[2][kClasses] = {};
-    size_t smem[2][kClasses] = {};
-    int grid[2][kClasses] = {};
+    std::vector<TableLaunch> launches;
     std::vector<gmle_group> plain;  // groups fitted by their own plain launch
 };
 
 // Groups of at least this many ROIs fill the GPU on their own: a batch
-// submission gives them their (autotuned) plain launch instead of the
-// persistent kernel; the serving loop keeps every request in the persistent
-// launches, whose captured graphs must not depend on request pointers.
+// submission gives them their (autotuned) plain launch instead of a table
+// launch; the serving loop keeps every request in the table launches, whose
+// captured graphs must not depend on request pointers.
 constexpr int64_t kPlainGroupRois = 65536;
 
 struct Server;
@@ -122,30 +136,33 @@ int nparams(int model);
 
 gmle_status init_mixed_set(gmle_ctx *ctx, MixedSet &m);
 void free_mixed_set(MixedSet &m);
-// Validate the groups and fill the pinned tables of every (family, class);
-// with allow_plain, groups of kPlainGroupRois or more go to plan.plain.
+// How a table launch picks its shape: from the context's tuning for the
+// kind, else the size-based default for `shape_rois` ROIs (0: the kind's ROIs
+// in this submission).  Persistent grids are full (SMs x resident blocks)
+// when `full_grid`, else no larger than the tiles.
+struct PlanOptions {
+    bool allow_plain = true;
+    int64_t shape_rois = 0;
+    bool full_grid = false;
+    // table capacity to reserve: groups, and tiles for this many ROIs
+    int64_t reserve_groups = 0, reserve_rois = 0;
+};
+// Validate the groups and fill the pinned tables of every kind present.
 gmle_status plan_mixed(gmle_ctx *ctx, const gmle_group *groups, int32_t ngroups, MixedSet &m,
-                       MixedPlan &plan, bool allow_plain);
-// Copy the plan's tables to the device on s (not part of a captured graph);
-// with record_reuse each table's reuse event is recorded after its copy.
+                       MixedPlan &plan, const PlanOptions &opt);
+// Copy the plan's tables to the device on s (not for zero-copy sets); with
+// record_reuse each table's reuse event is recorded after its copy.
 gmle_status upload_plan(gmle_ctx *ctx, MixedSet &m, const MixedPlan &plan, cudaStream_t s,
                         bool record_reuse);
-// The plan's plain launches on s, then one persistent launch per (family,
-// class), the classes concurrently on m.fork, joined back into s.
+// The plan's plain launches on s, then its table launches, concurrently on
+// m.fork when there are several, joined back into s.
 gmle_status enqueue_plan(gmle_ctx *ctx, MixedSet &m, const MixedPlan &plan, cudaStream_t s);
 gmle_status validate_groups(gmle_ctx *ctx, const gmle_group *groups, int32_t ngroups);
-gmle_status ensure_mixed(gmle_ctx *ctx, MixedBufs &b, int ngroups);
-// Fill b's pinned table for one camera family, with tiles of `tile` ROIs;
-// returns its number of tiles.
-int64_t build_mixed_table(gmle_ctx *ctx, const gmle_group *groups, int32_t ngroups, bool scmos,
-                          int tile, MixedBufs &b, gmle_status *st);
-// Counter reset and kernel launch of class `cls` over the table in b (the
-// caller records b.reuse, or keeps b untouched until the launch has finished).
-gmle_status enqueue_mixed(gmle_ctx *ctx, bool scmos, int cls, MixedBufs &b, size_t smem, int grid,
-                          cudaStream_t s, bool zero_copy);
-int mixed_grid(gmle_ctx *ctx, bool scmos, int cls, size_t smem);
-gmle_status free_mixed(MixedBufs &b);
-size_t mixed_smem(const gmle_group *groups, int32_t ngroups, bool scmos, int tile);
+Tuning pick_tuning(gmle_ctx *ctx, const gmle_fit_desc *d, int64_t n);
+Tuning default_tuning(int num_sms, int model, int box, bool scmos, int64_t n);
+gmle::KernelArgs make_args(gmle_ctx *ctx, const gmle_fit_desc *d, const float *data,
+                           const int32_t *xc, const int32_t *yc, int64_t n, float *params,
+                           float *crlb, float *llr, uint8_t *flags, int tpr);
 
 void server_destroy(gmle_ctx *ctx);
 

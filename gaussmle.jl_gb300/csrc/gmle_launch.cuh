@@ -1,7 +1,7 @@
 // gmle_launch.cuh - launch of one fit-kernel specialisation.  Each
-// gmle_fit_<model>.cu translation unit instantiates the kernels of one PSF
-// model for every supported box size and camera family, so the four units
-// compile in parallel.
+// gmle_fit_<model>_<camera family>.cu translation unit instantiates the
+// kernels of one PSF model and camera family for every supported box size, so
+// the eight units compile in parallel.
 #pragma once
 
 #include "gmle_fit_kernel.cuh"
@@ -10,68 +10,156 @@ namespace gmle {
 
 // Box sizes with a compiled specialisation (the configurations use 7..15).
 constexpr int kBoxes[] = {5, 7, 9, 11, 13, 15};
+constexpr int kNumBoxes = 6;
 
-inline bool box_supported(int box)
+__host__ __device__ constexpr int box_index(int box)
 {
-    for (int b : kBoxes)
-        if (b == box) return true;
-    return false;
+    return box == 5 ? 0 : box == 7 ? 1 : box == 9 ? 2 : box == 11 ? 3 : box == 13 ? 4
+                                                                     : box == 15 ? 5 : -1;
 }
 
-cudaError_t launch_fit_model0(int box, bool scmos, const KernelArgs &a, int rois_per_block,
-                              cudaStream_t s);
-cudaError_t launch_fit_model1(int box, bool scmos, const KernelArgs &a, int rois_per_block,
-                              cudaStream_t s);
-cudaError_t launch_fit_model2(int box, bool scmos, const KernelArgs &a, int rois_per_block,
-                              cudaStream_t s);
-cudaError_t launch_fit_model3(int box, bool scmos, const KernelArgs &a, int rois_per_block,
-                              cudaStream_t s);
+inline bool box_supported(int box) { return box_index(box) >= 0; }
 
 // Largest block of the one-thread-per-ROI kernel (its __launch_bounds__).
 constexpr int kMaxThreadsR1 = 64;
 
-template <int MODEL, int BOX, bool SCMOS>
-cudaError_t launch_one(const KernelArgs &a, int rois_per_block, cudaStream_t s)
+// One launch of a model's kernel.  Plain (t.header == nullptr): ceil(a.n / rpb)
+// blocks over `a`.  Table: `grid` persistent blocks over the table's groups,
+// whose arguments carry this launch's tpr; `a` then only supplies tpr.
+struct LaunchShape {
+    int tpr;
+    int rois_per_block;
+    int64_t grid;  // table launches only
+};
+
+#define GMLE_DECLARE_FAMILY(M, FAM)                                                           \
+    cudaError_t launch_fit_m##M##_##FAM(int box, const KernelArgs &a, const TileTable &t,     \
+                                        const LaunchShape &shape, cudaStream_t s);            \
+    int table_blocks_m##M##_##FAM(int box, int tpr, int rois_per_block);
+GMLE_DECLARE_FAMILY(0, poisson) GMLE_DECLARE_FAMILY(0, scmos)
+GMLE_DECLARE_FAMILY(1, poisson) GMLE_DECLARE_FAMILY(1, scmos)
+GMLE_DECLARE_FAMILY(2, poisson) GMLE_DECLARE_FAMILY(2, scmos)
+GMLE_DECLARE_FAMILY(3, poisson) GMLE_DECLARE_FAMILY(3, scmos)
+#undef GMLE_DECLARE_FAMILY
+
+inline cudaError_t launch_fit(int model, int box, bool scmos, const KernelArgs &a,
+                              const TileTable &t, const LaunchShape &shape, cudaStream_t s)
 {
-    const int threads = rois_per_block * a.tpr;
-    const size_t smem = smem_bytes(MODEL, BOX, SCMOS, a.tpr, rois_per_block);
-    const bool r1 = a.tpr == 1;
-    if (r1 && threads > kMaxThreadsR1) return cudaErrorInvalidConfiguration;
-    void (*kern)(const KernelArgs) = r1 ? fit_kernel_r1<MODEL, BOX, SCMOS>
-                                        : fit_kernel<MODEL, BOX, SCMOS>;
-    static bool attr_done[2] = {false, false};  // per specialisation and kernel
-    if (!attr_done[r1]) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             227 * 1024);
-        if (e != cudaSuccess) return e;
-        attr_done[r1] = true;
+#define GMLE_CASE(M)                                                        \
+    case M:                                                                 \
+        return scmos ? launch_fit_m##M##_scmos(box, a, t, shape, s)         \
+                     : launch_fit_m##M##_poisson(box, a, t, shape, s);
+    switch (model) {
+        GMLE_CASE(0) GMLE_CASE(1) GMLE_CASE(2) GMLE_CASE(3)
+        default: return cudaErrorInvalidValue;
     }
-    const int64_t blocks = (a.n + rois_per_block - 1) / rois_per_block;
+#undef GMLE_CASE
+}
+
+// Resident blocks per SM of a table launch of this shape (0 on error); also
+// sets the kernel's shared-memory limit on the current device.
+inline int table_blocks_per_sm(int model, int box, bool scmos, int tpr, int rois_per_block)
+{
+#define GMLE_CASE(M)                                                        \
+    case M:                                                                 \
+        return scmos ? table_blocks_m##M##_scmos(box, tpr, rois_per_block)  \
+                     : table_blocks_m##M##_poisson(box, tpr, rois_per_block);
+    switch (model) {
+        GMLE_CASE(0) GMLE_CASE(1) GMLE_CASE(2) GMLE_CASE(3)
+        default: return 0;
+    }
+#undef GMLE_CASE
+}
+
+// Dynamic shared memory of a launch (table launches add the block's slot).
+inline size_t launch_smem(int model, int box, bool scmos, int tpr, int rpb, bool table)
+{
+    const size_t s = smem_bytes(model, box, scmos, tpr, rpb);
+    return table ? table_smem_bytes(s) : s;
+}
+
+using FitKernel = void (*)(const KernelArgs, const TileTable);
+
+template <int MODEL, int BOX, bool SCMOS>
+cudaError_t kernel_for(int tpr, bool table, FitKernel *kern)
+{
+    const bool r1 = tpr == 1;
+    *kern = r1 ? (table ? fit_kernel_r1<MODEL, BOX, SCMOS, true> : fit_kernel_r1<MODEL, BOX, SCMOS, false>)
+               : (table ? fit_kernel<MODEL, BOX, SCMOS, true> : fit_kernel<MODEL, BOX, SCMOS, false>);
+    // The largest dynamic shared memory any shape asks for, once per kernel
+    // and device (setting it twice is harmless).
+    constexpr int kMaxDevices = 64;
+    static bool done[2][2][kMaxDevices] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const bool known = dev >= 0 && dev < kMaxDevices;
+    if (known && done[r1][table][dev]) return cudaSuccess;
+    e = cudaFuncSetAttribute(*kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    if (e == cudaSuccess && known) done[r1][table][dev] = true;
+    return e;
+}
+
+template <int MODEL, int BOX, bool SCMOS>
+cudaError_t launch_one(const KernelArgs &a, const TileTable &t, const LaunchShape &shape,
+                       cudaStream_t s)
+{
+    const int tpr = shape.tpr, rpb = shape.rois_per_block;
+    if (tpr != a.tpr) return cudaErrorInvalidValue;
+    const int threads = rpb * tpr;
+    const bool table = t.header != nullptr;
+    if (tpr == 1 && threads > kMaxThreadsR1) return cudaErrorInvalidConfiguration;
+    const size_t smem = launch_smem(MODEL, BOX, SCMOS, tpr, rpb, table);
+    FitKernel kern;
+    cudaError_t e = kernel_for<MODEL, BOX, SCMOS>(tpr, table, &kern);
+    if (e != cudaSuccess) return e;
+    const int64_t blocks = table ? shape.grid : (a.n + rpb - 1) / rpb;
     if (blocks <= 0) return cudaSuccess;
     if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-    kern<<<(unsigned)blocks, threads, smem, s>>>(a);
+    kern<<<(unsigned)blocks, threads, smem, s>>>(a, t);
     return cudaGetLastError();
 }
 
-template <int MODEL>
-cudaError_t launch_model(int box, bool scmos, const KernelArgs &a, int rois_per_block,
-                         cudaStream_t s)
+template <int MODEL, int BOX, bool SCMOS>
+int table_blocks_one(int tpr, int rpb)
 {
-#define GMLE_CASE(B)                                                                     \
-    case B:                                                                              \
-        return scmos ? launch_one<MODEL, B, true>(a, rois_per_block, s)                  \
-                     : launch_one<MODEL, B, false>(a, rois_per_block, s);
-    switch (box) {
-        GMLE_CASE(5)
-        GMLE_CASE(7)
-        GMLE_CASE(9)
-        GMLE_CASE(11)
-        GMLE_CASE(13)
-        GMLE_CASE(15)
-        default:
-            return cudaErrorInvalidValue;
+    FitKernel kern;
+    if (kernel_for<MODEL, BOX, SCMOS>(tpr, true, &kern) != cudaSuccess) return 0;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &nb, kern, rpb * tpr, launch_smem(MODEL, BOX, SCMOS, tpr, rpb, true)) != cudaSuccess)
+        return 0;
+    return nb;
+}
+
+#define GMLE_BOX_SWITCH(CALL)       \
+    switch (box) {                  \
+        case 5: CALL(5)             \
+        case 7: CALL(7)             \
+        case 9: CALL(9)             \
+        case 11: CALL(11)           \
+        case 13: CALL(13)           \
+        case 15: CALL(15)           \
+        default: break;             \
     }
+
+template <int MODEL, bool SCMOS>
+cudaError_t launch_family(int box, const KernelArgs &a, const TileTable &t,
+                          const LaunchShape &shape, cudaStream_t s)
+{
+#define GMLE_CASE(B) return launch_one<MODEL, B, SCMOS>(a, t, shape, s);
+    GMLE_BOX_SWITCH(GMLE_CASE)
 #undef GMLE_CASE
+    return cudaErrorInvalidValue;
+}
+
+template <int MODEL, bool SCMOS>
+int table_blocks_family(int box, int tpr, int rpb)
+{
+#define GMLE_CASE(B) return table_blocks_one<MODEL, B, SCMOS>(tpr, rpb);
+    GMLE_BOX_SWITCH(GMLE_CASE)
+#undef GMLE_CASE
+    return 0;
 }
 
 }  // namespace gmle

@@ -1,27 +1,32 @@
 // gmle_noalloc.cu - gmle_fit_mixed_device_noalloc: the mixed-batch fit for
 // callers that cannot allocate device memory.
 //
-// The persistent mixed-batch kernels (gmle_mixed.cuh) need scratch beyond the
-// caller's inputs and outputs: a group table and a header per launch, a
-// work-stealing tile counter per launch, and a counter of skipped ROIs.  Here
-// that scratch is the file-scope array g_noalloc_scratch, reserved on a device
-// when this module is loaded there and held until the process exits:
+// A mixed batch runs as one persistent table launch per (camera family, PSF
+// model, box size) present (gmle_fit_kernel.cuh, TileTable).  Those launches
+// need scratch beyond the caller's inputs and outputs: per launch a header and
+// a work-stealing tile counter, per group its kernel arguments and first
+// tile, and a counter of skipped ROIs.  Here that scratch is the file-scope
+// array g_noalloc_scratch, reserved on a device when this module is loaded
+// there and held until the process exits:
 //
-//   [0, 256)    unsigned long long counters[8]: the tile counters of the six
-//               (camera family, shared-memory class) launches, then the
-//               skipped-ROI counter.  A tile counter must be zero when its
-//               launch starts; every call's table copy writes all of them to
-//               zero, on the caller's stream, before its launches.
-//   [256, 512)  int64_t headers[6][2]: {groups, tiles} of each launch.
-//   [512, ...)  gmle::GroupDesc table[GMLE_NOALLOC_MAX_GROUPS]; each launch
-//               reads its own contiguous slice.
+//   [0, 512)       unsigned long long counters[64]: the tile counters of the
+//                  48 kinds, then the skipped-ROI counter.  A tile counter must
+//                  be zero when its launch starts; every call's table copy
+//                  writes all of them to zero, on the caller's stream, before
+//                  its launches.
+//   [512, 1536)    int64_t headers[48][2]: {groups, tiles} of each launch.
+//   [1536, 9728)   int64_t tile0[GMLE_NOALLOC_MAX_GROUPS]: each group's first
+//                  tile within its launch (the tile's group is found by
+//                  binary search, so no per-tile table is needed).
+//   [9728, ...)    gmle::KernelArgs args[GMLE_NOALLOC_MAX_GROUPS].
+// Each launch reads its own contiguous slice of tile0 and args.
 //
-// A call builds the image of [0, 512 + 192 * groups) in a static host buffer,
+// A call builds the image of [0, 9728 + 224 * groups) in a static host buffer,
 // copies it with one cudaMemcpyAsync on the caller's stream (the pageable
 // source is consumed before that call returns, so the buffer is reused by the
-// next call), then enqueues one persistent launch per (family, class) present
-// on the same stream.  It allocates nothing: no cudaMalloc, cudaMallocHost,
-// cudaFree, stream or event, and no host heap.
+// next call), then enqueues the launches on the same stream.  It allocates
+// nothing: no cudaMalloc, cudaMallocHost, cudaFree, stream or event, and no
+// host heap.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -34,20 +39,22 @@
 
 namespace {
 
-using gmle::GroupDesc;
+using gmle::KernelArgs;
+using gmle_rt::kKinds;
 
 constexpr int kMaxGroups = GMLE_NOALLOC_MAX_GROUPS;
-constexpr int kLaunches = 2 * gmle_rt::kClasses;  // (camera family, shared-memory class)
-constexpr size_t kHeadersOff = 256;
-constexpr size_t kTableOff = 512;
-constexpr size_t kScratchBytes = kTableOff + sizeof(GroupDesc) * kMaxGroups;
-constexpr int kBadCounter = kLaunches;            // index in counters[]
+constexpr size_t kCountersOff = 0;
+constexpr int kBadCounter = kKinds;  // index in counters[]
+constexpr size_t kHeadersOff = 512;
+constexpr size_t kTile0Off = 1536;
+constexpr size_t kArgsOff = kTile0Off + sizeof(int64_t) * kMaxGroups;
+constexpr size_t kScratchBytes = kArgsOff + sizeof(KernelArgs) * kMaxGroups;
 constexpr int kMaxDevices = 64;
 
 static_assert(kScratchBytes == GMLE_NOALLOC_SCRATCH_BYTES, "header and layout disagree");
-static_assert(sizeof(unsigned long long) * (kLaunches + 1) <= kHeadersOff, "counters overflow");
-static_assert(sizeof(int64_t) * 2 * kLaunches <= kTableOff - kHeadersOff, "headers overflow");
-static_assert(sizeof(GroupDesc) % 16 == 0, "table entries keep 16-byte alignment");
+static_assert(sizeof(unsigned long long) * (kKinds + 1) <= kHeadersOff, "counters overflow");
+static_assert(kHeadersOff + sizeof(int64_t) * 2 * kKinds <= kTile0Off, "headers overflow");
+static_assert(sizeof(KernelArgs) % 16 == 0 && kArgsOff % 16 == 0, "16-byte aligned arguments");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -85,9 +92,9 @@ gmle_status check_group(const gmle_group &G, int k, bool have_var, bool have_adu
     if (d.model < 0 || d.model > 3)
         return report(err, err_len, GMLE_UNSUPPORTED_MODEL, "group %d: unknown model id %d", k,
                       d.model);
-    if (!gmle::mixed_box(d.box))
+    if (!gmle::box_supported(d.box))
         return report(err, err_len, GMLE_UNSUPPORTED_BOX,
-                      "group %d: box %d not in the mixed kernel (5..15 odd)", k, d.box);
+                      "group %d: box size %d has no compiled kernel (5..15 odd)", k, d.box);
     if (d.iterations < 0) return report(err, err_len, GMLE_INVALID_ARG, "group %d: iterations < 0", k);
     if (d.camera < 0 || d.camera > 2)
         return report(err, err_len, GMLE_INVALID_ARG, "group %d: unknown camera id %d", k, d.camera);
@@ -115,13 +122,8 @@ gmle_status check_group(const gmle_group &G, int k, bool have_var, bool have_adu
     return GMLE_OK;
 }
 
-double group_cost(const gmle_fit_desc &d)
-{
-    return (double)d.box * d.box * (gmle_rt::nparams(d.model) + (d.model == 3 ? 3 : 0));
-}
-
-// First call on the current device: the scratch address and the kernels'
-// shared-memory limit.  Called with g_mu held.
+// First call on the current device: the scratch address and the SM count.
+// Called with g_mu held.
 gmle_status setup_device(int dev, char *err, int32_t err_len)
 {
     DeviceState &S = g_dev[dev];
@@ -132,9 +134,6 @@ gmle_status setup_device(int dev, char *err, int32_t err_len)
     int sms = 0;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return cuda_report(err, err_len, e, "cudaDeviceGetAttribute");
-    e = gmle::mixed_set_attributes_poisson();
-    if (e == cudaSuccess) e = gmle::mixed_set_attributes_scmos();
-    if (e != cudaSuccess) return cuda_report(err, err_len, e, "cudaFuncSetAttribute(mixed kernels)");
     S.num_sms = sms;
     S.scratch = static_cast<unsigned char *>(p);
     return GMLE_OK;
@@ -174,90 +173,93 @@ extern "C" gmle_status gmle_fit_mixed_device_noalloc(const gmle_group *groups, i
     if (st != GMLE_OK) return st;
     const DeviceState &S = g_dev[dev];
 
-    // Host image: zeroed counters, then per launch its header and table slice
-    // (groups in decreasing cost, so that the heavy tiles start first).
-    std::memset(g_stage, 0, kTableOff);
-    unsigned long long *d_counters = reinterpret_cast<unsigned long long *>(S.scratch);
+    // Host image: zeroed counters, then per kind its header and its slice of
+    // the group arguments and first tiles.
+    std::memset(g_stage, 0, kTile0Off);
     int64_t *h_headers = reinterpret_cast<int64_t *>(g_stage + kHeadersOff);
-    GroupDesc *h_table = reinterpret_cast<GroupDesc *>(g_stage + kTableOff);
+    int64_t *h_tile0 = reinterpret_cast<int64_t *>(g_stage + kTile0Off);
+    KernelArgs *h_args = reinterpret_cast<KernelArgs *>(g_stage + kArgsOff);
+    unsigned long long *d_counters = reinterpret_cast<unsigned long long *>(S.scratch + kCountersOff);
     int used = 0;
-    int first[kLaunches] = {};
-    size_t smem[kLaunches] = {};
-    for (int fam = 0; fam < 2; fam++) {
-        for (int c = 0; c < gmle_rt::kClasses; c++) {
-            const int L = fam * gmle_rt::kClasses + c;
-            const int tile = gmle::class_tile(c);
-            int cnt = 0;
-            for (int k = 0; k < ngroups; k++) {
-                const gmle_group &G = groups[k];
-                if (G.n > 0 && (G.desc.camera != GMLE_CAMERA_POISSON) == (fam == 1) &&
-                    gmle::box_class(G.desc.box) == c)
-                    g_order[cnt++] = k;
+    int first[kKinds] = {};
+    gmle::LaunchShape shape[kKinds] = {};
+    for (int kind = 0; kind < kKinds; kind++) {
+        int cnt = 0;
+        int64_t rois = 0;
+        for (int k = 0; k < ngroups; k++)
+            if (groups[k].n > 0 && gmle_rt::kind_of(groups[k].desc) == kind) {
+                g_order[cnt++] = k;
+                rois += groups[k].n;
             }
-            first[L] = used;
-            if (cnt == 0) continue;
-            std::sort(g_order, g_order + cnt, [&](int x, int y) {
-                const double cx = group_cost(groups[x].desc), cy = group_cost(groups[y].desc);
-                return cx > cy || (cx == cy && x < y);
-            });
-            int64_t tiles = 0;
-            for (int q = 0; q < cnt; q++) {
-                const gmle_group &G = groups[g_order[q]];
-                GroupDesc &D = h_table[used + q];
-                std::memset(&D, 0, sizeof D);
-                D.data = G.data;
-                D.xc = G.x_corners;
-                D.yc = G.y_corners;
-                D.n = G.n;
-                D.params = G.params;
-                D.crlb = G.crlb;
-                D.llr = G.llr;
-                D.flags = G.flags;
-                D.model = G.desc.model;
-                D.box = G.desc.box;
-                D.iterations = G.desc.iterations;
-                D.adu = G.desc.camera == GMLE_CAMERA_SCMOS_ADU;
-                std::memcpy(D.psf, G.desc.psf, sizeof D.psf);
-                std::memcpy(D.lower, G.desc.lower, sizeof D.lower);
-                std::memcpy(D.upper, G.desc.upper, sizeof D.upper);
-                std::memcpy(D.max_step, G.desc.max_step, sizeof D.max_step);
-                D.tile0 = tiles;
-                tiles += (G.n + tile - 1) / tile;
-                smem[L] = std::max(smem[L], gmle::smem_bytes(G.desc.model, G.desc.box, fam == 1, 1,
-                                                             tile));
-            }
-            h_headers[2 * L] = cnt;
-            h_headers[2 * L + 1] = tiles;
-            used += cnt;
+        first[kind] = used;
+        if (cnt == 0) continue;
+        const gmle_fit_desc &d0 = groups[g_order[0]].desc;
+        const bool scmos = d0.camera != GMLE_CAMERA_POISSON;
+        const gmle_rt::Tuning t = gmle_rt::default_tuning(S.num_sms, d0.model, d0.box, scmos, rois);
+        int64_t tiles = 0;
+        for (int q = 0; q < cnt; q++) {
+            const gmle_group &G = groups[g_order[q]];
+            KernelArgs &A = h_args[used + q];
+            std::memset(&A, 0, sizeof A);
+            A.data = G.data;
+            A.xc = G.x_corners;
+            A.yc = G.y_corners;
+            A.n = G.n;
+            A.var = variance;
+            A.gain = gain;
+            A.offset = offset;
+            A.ny = variance ? ny : 0;
+            A.nx = variance ? nx : 0;
+            A.adu = G.desc.camera == GMLE_CAMERA_SCMOS_ADU;
+            A.iterations = G.desc.iterations;
+            A.tpr = t.tpr;
+            A.sqrt2pi = sqrtf(2.0f * (float)3.14159265358979323846);
+            std::memcpy(A.psf, G.desc.psf, sizeof A.psf);
+            std::memcpy(A.lower, G.desc.lower, sizeof A.lower);
+            std::memcpy(A.upper, G.desc.upper, sizeof A.upper);
+            std::memcpy(A.max_step, G.desc.max_step, sizeof A.max_step);
+            A.params = G.params;
+            A.crlb = G.crlb;
+            A.llr = G.llr;
+            A.flags = G.flags;
+            A.bad_corners = d_counters + kBadCounter;
+            h_tile0[used + q] = tiles;
+            tiles += (G.n + t.rois_per_block - 1) / t.rois_per_block;
         }
+        h_headers[2 * kind] = cnt;
+        h_headers[2 * kind + 1] = tiles;
+        const int bps = gmle::table_blocks_per_sm(d0.model, d0.box, scmos, t.tpr, t.rois_per_block);
+        if (bps <= 0)
+            return report(err, err_len, GMLE_CUDA_ERROR,
+                          "no resident block for model %d box %d (tpr %d, %d ROIs)", d0.model,
+                          d0.box, t.tpr, t.rois_per_block);
+        shape[kind] = gmle::LaunchShape{t.tpr, t.rois_per_block,
+                                        std::min<int64_t>((int64_t)S.num_sms * bps, tiles)};
+        used += cnt;
     }
     if (used == 0) return GMLE_OK;
 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    e = cudaMemcpyAsync(S.scratch, g_stage, kTableOff + sizeof(GroupDesc) * (size_t)used,
+    e = cudaMemcpyAsync(S.scratch, g_stage, kArgsOff + sizeof(KernelArgs) * (size_t)used,
                         cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return cuda_report(err, err_len, e, "H2D group tables");
-    for (int fam = 0; fam < 2; fam++) {
-        for (int c = 0; c < gmle_rt::kClasses; c++) {
-            const int L = fam * gmle_rt::kClasses + c;
-            if (h_headers[2 * L] == 0) continue;
-            const bool scmos = fam == 1;
-            gmle::MixedArgs m;
-            m.groups = reinterpret_cast<const GroupDesc *>(S.scratch + kTableOff) + first[L];
-            m.header = reinterpret_cast<const int64_t *>(S.scratch + kHeadersOff) + 2 * L;
-            m.tile_counter = d_counters + L;
-            m.var = variance;
-            m.gain = gain;
-            m.offset = offset;
-            m.ny = variance ? ny : 0;
-            m.nx = variance ? nx : 0;
-            m.rois_per_tile = gmle::class_tile(c);
-            m.sqrt2pi = sqrtf(2.0f * (float)3.14159265358979323846);
-            m.bad_corners = d_counters + kBadCounter;
-            const int grid = S.num_sms * std::max(1, gmle::mixed_blocks_per_sm(scmos, c, smem[L]));
-            e = gmle::launch_mixed(scmos, c, m, smem[L], grid, s);
-            if (e != cudaSuccess) return cuda_report(err, err_len, e, "mixed kernel launch");
-        }
+    for (int kind = 0; kind < kKinds; kind++) {
+        if (h_headers[2 * kind] == 0) continue;
+        const KernelArgs &A0 = h_args[first[kind]];
+        const int model = (kind / gmle::kNumBoxes) % 4;
+        const int box = gmle::kBoxes[kind % gmle::kNumBoxes];
+        const bool scmos = kind >= kKinds / 2;
+        gmle::TileTable t;
+        t.header = reinterpret_cast<const int64_t *>(S.scratch + kHeadersOff) + 2 * kind;
+        t.groups = reinterpret_cast<const KernelArgs *>(S.scratch + kArgsOff) + first[kind];
+        t.tiles = nullptr;
+        t.tile0 = reinterpret_cast<const int64_t *>(S.scratch + kTile0Off) + first[kind];
+        t.counter = d_counters + kind;
+        KernelArgs a;
+        std::memset(&a, 0, sizeof a);
+        a.tpr = A0.tpr;
+        e = gmle::launch_fit(model, box, scmos, a, t, shape[kind], s);
+        if (e != cudaSuccess) return cuda_report(err, err_len, e, "table launch");
     }
     return GMLE_OK;
 }

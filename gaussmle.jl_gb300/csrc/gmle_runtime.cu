@@ -75,11 +75,11 @@ gmle_status check_desc(gmle_ctx *ctx, const gmle_fit_desc *d)
 
 }  // namespace gmle_rt
 
-namespace {
+namespace gmle_rt {
 
 // Launch shape: enough threads to fill the GPU (threads per ROI grows for small
 // batches), and ROIs per block bounded by shared memory.
-Tuning default_tuning(const gmle_ctx *ctx, int model, int box, bool scmos, int64_t n)
+Tuning default_tuning(int num_sms, int model, int box, bool scmos, int64_t n)
 {
     // Resident ROIs per SM are bounded by shared memory; threads per ROI grow
     // until about 16 warps per SM are resident and the batch fills the GPU.
@@ -88,7 +88,7 @@ Tuning default_tuning(const gmle_ctx *ctx, int model, int box, bool scmos, int64
     const int64_t want_threads_sm = 512;
     int tpr = 1;
     while (tpr < 4 && (rois_per_sm * tpr < want_threads_sm ||
-                       n * tpr < (int64_t)ctx->num_sms * want_threads_sm))
+                       n * tpr < (int64_t)num_sms * want_threads_sm))
         tpr *= 2;
     int rpb = tpr == 1 ? 32 : 128 / tpr;
     while (rpb * tpr > 32 && gmle::smem_bytes(model, box, scmos, tpr, rpb) > 100 * 1024) rpb /= 2;
@@ -96,12 +96,16 @@ Tuning default_tuning(const gmle_ctx *ctx, int model, int box, bool scmos, int64
     return {tpr, rpb};
 }
 
+}  // namespace gmle_rt
+
+namespace gmle_rt {
+
 Tuning pick_tuning(gmle_ctx *ctx, const gmle_fit_desc *d, int64_t n)
 {
     const bool scmos = d->camera != GMLE_CAMERA_POISSON;
     auto it = ctx->tuning.find({d->model, d->box, (int)scmos});
     if (it != ctx->tuning.end()) return it->second;
-    return default_tuning(ctx, d->model, d->box, scmos, n);
+    return default_tuning(ctx->num_sms, d->model, d->box, scmos, n);
 }
 
 KernelArgs make_args(gmle_ctx *ctx, const gmle_fit_desc *d, const float *data, const int32_t *xc,
@@ -136,17 +140,17 @@ KernelArgs make_args(gmle_ctx *ctx, const gmle_fit_desc *d, const float *data, c
     return a;
 }
 
+}  // namespace gmle_rt
+
+namespace {
+
 cudaError_t launch(gmle_ctx *ctx, const gmle_fit_desc *d, const KernelArgs &a, int rpb,
                    cudaStream_t s)
 {
     const bool scmos = d->camera != GMLE_CAMERA_POISSON;
     ctx->launches++;
-    switch (d->model) {
-        case 0: return gmle::launch_fit_model0(d->box, scmos, a, rpb, s);
-        case 1: return gmle::launch_fit_model1(d->box, scmos, a, rpb, s);
-        case 2: return gmle::launch_fit_model2(d->box, scmos, a, rpb, s);
-        default: return gmle::launch_fit_model3(d->box, scmos, a, rpb, s);
-    }
+    return gmle::launch_fit(d->model, d->box, scmos, a, gmle::TileTable{},
+                            gmle::LaunchShape{a.tpr, rpb, 0}, s);
 }
 
 bool is_pinned(const void *p)
@@ -475,7 +479,7 @@ gmle_status gmle_get_tuning(gmle_ctx *ctx, int32_t model, int32_t box, int32_t c
     const bool scmos = camera != GMLE_CAMERA_POISSON;
     auto it = ctx->tuning.find({model, box, (int)scmos});
     Tuning t = it != ctx->tuning.end() ? it->second
-                                       : default_tuning(ctx, model, box, scmos, 1ll << 40);
+                                       : default_tuning(ctx->num_sms, model, box, scmos, 1ll << 40);
     *threads_per_roi = t.tpr;
     *rois_per_block = t.rois_per_block;
     return GMLE_OK;
@@ -567,65 +571,45 @@ gmle_status gmle_autotune(gmle_ctx *ctx, const gmle_fit_desc *desc, const float 
 
 }  // extern "C"
 
-// ---- mixed batches: one persistent work-stealing launch per camera family ------
+// ---- mixed batches: one persistent table launch per (family, model, box) ----------
 
 namespace gmle_rt {
 
 namespace {
 
-double group_cost(const gmle_fit_desc &d)
-{
-    return (double)d.box * d.box * (nparams(d.model) + (d.model == 3 ? 3 : 0));
-}
-
-}  // namespace
-
-gmle_status ensure_mixed(gmle_ctx *ctx, MixedBufs &b, int ngroups)
-{
-    if (!b.reuse) {
-        CK(cudaEventCreateWithFlags(&b.reuse, cudaEventDisableTiming), "cudaEventCreate");
-        CK(cudaMalloc(&b.d_counter, sizeof(unsigned long long)), "cudaMalloc(counter)");
-    }
-    if (b.cap < ngroups) {
-        CK(cudaEventSynchronize(b.reuse), "cudaEventSynchronize");
-        cudaFreeHost(b.h_base);
-        cudaFree(b.d_base);
-        b.h_base = b.d_base = nullptr;
-        b.cap = 0;
-        const int cap = std::max(64, ngroups);
-        const size_t bytes = kTableHeader + sizeof(gmle::GroupDesc) * cap;
-        CK(cudaMallocHost(&b.h_base, bytes), "cudaMallocHost(group table)");
-        CK(cudaMalloc(&b.d_base, bytes), "cudaMalloc(group table)");
-        b.h_header = reinterpret_cast<int64_t *>(b.h_base);
-        b.d_header = reinterpret_cast<int64_t *>(b.d_base);
-        b.h_groups = reinterpret_cast<gmle::GroupDesc *>(b.h_base + kTableHeader);
-        b.d_groups = reinterpret_cast<gmle::GroupDesc *>(b.d_base + kTableHeader);
-        b.cap = cap;
-    }
-    return GMLE_OK;
-}
-
-gmle_status free_mixed(MixedBufs &b)
+void free_table(TableBufs &b)
 {
     if (b.reuse) cudaEventSynchronize(b.reuse);
     cudaFreeHost(b.h_base);
     cudaFree(b.d_base);
     cudaFree(b.d_counter);
     if (b.reuse) cudaEventDestroy(b.reuse);
-    b = MixedBufs();
+    if (b.used) cudaEventDestroy(b.used);
+    b = TableBufs();
+}
+
+// Room for `groups` groups and `tiles` tiles (grown by half again when short).
+gmle_status ensure_table(gmle_ctx *ctx, TableBufs &b, int64_t groups, int64_t tiles)
+{
+    if (!b.reuse) {
+        CK(cudaEventCreateWithFlags(&b.reuse, cudaEventDisableTiming), "cudaEventCreate");
+        CK(cudaEventCreateWithFlags(&b.used, cudaEventDisableTiming), "cudaEventCreate");
+        CK(cudaMalloc(&b.d_counter, sizeof(unsigned long long)), "cudaMalloc(tile counter)");
+    }
+    if (b.cap_groups >= groups && b.cap_tiles >= tiles) return GMLE_OK;
+    CK(cudaEventSynchronize(b.reuse), "cudaEventSynchronize");
+    CK(cudaEventSynchronize(b.used), "cudaEventSynchronize");
+    cudaFreeHost(b.h_base);
+    cudaFree(b.d_base);
+    b.h_base = b.d_base = nullptr;
+    b.cap_groups = std::max<int64_t>({64, groups, b.cap_groups + b.cap_groups / 2});
+    b.cap_tiles = std::max<int64_t>({1024, tiles, b.cap_tiles + b.cap_tiles / 2});
+    CK(cudaMallocHost(&b.h_base, b.bytes()), "cudaMallocHost(group table)");
+    CK(cudaMalloc(&b.d_base, b.bytes()), "cudaMalloc(group table)");
     return GMLE_OK;
 }
 
-size_t mixed_smem(const gmle_group *groups, int32_t ngroups, bool scmos, int tile)
-{
-    size_t m = 0;
-    for (int k = 0; k < ngroups; k++) {
-        const gmle_fit_desc &d = groups[k].desc;
-        if ((d.camera != GMLE_CAMERA_POISSON) != scmos || groups[k].n <= 0) continue;
-        m = std::max(m, gmle::smem_bytes(d.model, d.box, scmos, 1, tile));
-    }
-    return m;
-}
+}  // namespace
 
 gmle_status validate_groups(gmle_ctx *ctx, const gmle_group *groups, int32_t ngroups)
 {
@@ -633,96 +617,21 @@ gmle_status validate_groups(gmle_ctx *ctx, const gmle_group *groups, int32_t ngr
         const gmle_group &G = groups[k];
         gmle_status st = check_desc(ctx, &G.desc);
         if (st != GMLE_OK) return st;
-        if (!gmle::mixed_box(G.desc.box))
-            return fail(ctx, GMLE_UNSUPPORTED_BOX, "group %d: box %d not in the mixed kernel", k,
-                        G.desc.box);
         if (G.n < 0) return fail(ctx, GMLE_INVALID_ARG, "group %d: n < 0", k);
         if (G.n > 0 && (!G.data || !G.params || !G.crlb || !G.llr))
             return fail(ctx, GMLE_INVALID_ARG, "group %d: data and output pointers are required", k);
         if (G.n > 0 && G.desc.camera != GMLE_CAMERA_POISSON && (!G.x_corners || !G.y_corners))
             return fail(ctx, GMLE_INVALID_ARG, "group %d: sCMOS fit needs ROI corners", k);
+        if (G.n > 0x7fffffffLL * 32)
+            return fail(ctx, GMLE_INVALID_ARG, "group %d: more ROIs than a table indexes", k);
     }
-    return GMLE_OK;
-}
-
-int64_t build_mixed_table(gmle_ctx *ctx, const gmle_group *groups, int32_t ngroups, bool scmos,
-                          int tile, MixedBufs &b, gmle_status *st)
-{
-    *st = GMLE_OK;
-    std::vector<int> idx;
-    for (int k = 0; k < ngroups; k++)
-        if ((groups[k].desc.camera != GMLE_CAMERA_POISSON) == scmos && groups[k].n > 0)
-            idx.push_back(k);
-    if (idx.empty()) return 0;
-    // most expensive ROIs first: the heavy tiles start early, the tail is short
-    std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) {
-        return group_cost(groups[x].desc) > group_cost(groups[y].desc);
-    });
-    *st = ensure_mixed(ctx, b, (int)idx.size());
-    if (*st != GMLE_OK) return 0;
-    if (cudaEventSynchronize(b.reuse) != cudaSuccess) {  // the pinned table is free
-        *st = cuda_fail(ctx, cudaGetLastError(), "cudaEventSynchronize");
-        return 0;
-    }
-    int64_t tiles = 0;
-    for (size_t q = 0; q < idx.size(); q++) {
-        const gmle_group &G = groups[idx[q]];
-        gmle::GroupDesc &D = b.h_groups[q];
-        D.data = G.data;
-        D.xc = G.x_corners;
-        D.yc = G.y_corners;
-        D.n = G.n;
-        D.params = G.params;
-        D.crlb = G.crlb;
-        D.llr = G.llr;
-        D.flags = G.flags;
-        D.model = G.desc.model;
-        D.box = G.desc.box;
-        D.iterations = G.desc.iterations;
-        D.adu = G.desc.camera == GMLE_CAMERA_SCMOS_ADU;
-        std::memcpy(D.psf, G.desc.psf, sizeof D.psf);
-        std::memcpy(D.lower, G.desc.lower, sizeof D.lower);
-        std::memcpy(D.upper, G.desc.upper, sizeof D.upper);
-        std::memcpy(D.max_step, G.desc.max_step, sizeof D.max_step);
-        D.tile0 = tiles;
-        tiles += (G.n + tile - 1) / tile;
-    }
-    b.h_header[0] = (int64_t)idx.size();
-    b.h_header[1] = tiles;
-    return tiles;
-}
-
-int mixed_grid(gmle_ctx *ctx, bool scmos, int cls, size_t smem)
-{
-    return ctx->num_sms * std::max(1, gmle::mixed_blocks_per_sm(scmos, cls, smem));
-}
-
-gmle_status enqueue_mixed(gmle_ctx *ctx, bool scmos, int cls, MixedBufs &b, size_t smem, int grid,
-                          cudaStream_t s, bool zero_copy)
-{
-    // The table sits at fixed device addresses (copied in by upload_plan), so
-    // a captured graph of these launches stays valid for any table contents.
-    CK(cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned long long), s), "reset tile counter");
-    gmle::MixedArgs m;
-    m.groups = zero_copy ? b.h_groups : b.d_groups;
-    m.header = zero_copy ? b.h_header : b.d_header;
-    m.tile_counter = b.d_counter;
-    m.var = ctx->d_var;
-    m.gain = ctx->d_gain;
-    m.offset = ctx->d_offset;
-    m.ny = ctx->ny;
-    m.nx = ctx->nx;
-    m.rois_per_tile = gmle::class_tile(cls);
-    m.sqrt2pi = sqrtf(2.0f * (float)3.14159265358979323846);
-    m.bad_corners = ctx->d_bad;
-    CK(gmle::launch_mixed(scmos, cls, m, smem, grid, s), "mixed kernel launch");
     return GMLE_OK;
 }
 
 gmle_status init_mixed_set(gmle_ctx *ctx, MixedSet &m)
 {
     if (m.ev_fork) return GMLE_OK;
-    for (int c = 0; c < kClasses; c++) {
+    for (int c = 0; c < kForks; c++) {
         CK(cudaStreamCreateWithFlags(&m.fork[c], cudaStreamNonBlocking), "cudaStreamCreate");
         CK(cudaEventCreateWithFlags(&m.ev_join[c], cudaEventDisableTiming), "cudaEventCreate");
     }
@@ -732,9 +641,8 @@ gmle_status init_mixed_set(gmle_ctx *ctx, MixedSet &m)
 
 void free_mixed_set(MixedSet &m)
 {
-    for (int f = 0; f < 2; f++)
-        for (int c = 0; c < kClasses; c++) free_mixed(m.bufs[f][c]);
-    for (int c = 0; c < kClasses; c++) {
+    for (TableBufs &b : m.tables) free_table(b);
+    for (int c = 0; c < kForks; c++) {
         if (m.fork[c]) {
             cudaStreamSynchronize(m.fork[c]);
             cudaStreamDestroy(m.fork[c]);
@@ -746,32 +654,64 @@ void free_mixed_set(MixedSet &m)
 }
 
 gmle_status plan_mixed(gmle_ctx *ctx, const gmle_group *groups, int32_t ngroups, MixedSet &m,
-                       MixedPlan &plan, bool allow_plain)
+                       MixedPlan &plan, const PlanOptions &opt)
 {
     gmle_status st = validate_groups(ctx, groups, ngroups);
     if (st != GMLE_OK) return st;
     plan = MixedPlan();
-    std::vector<gmle_group> sub;
-    for (int k = 0; k < ngroups; k++)
-        if (allow_plain && groups[k].n >= kPlainGroupRois) plan.plain.push_back(groups[k]);
-    for (int fam = 0; fam < 2; fam++) {
-        const bool scmos = fam == 1;
-        for (int c = 0; c < kClasses; c++) {
-            sub.clear();
-            for (int k = 0; k < ngroups; k++)
-                if (box_class(groups[k].desc.box) == c &&
-                    !(allow_plain && groups[k].n >= kPlainGroupRois))
-                    sub.push_back(groups[k]);
-            if (sub.empty()) continue;
-            const int tile = class_tile(c);
-            const int64_t tiles = build_mixed_table(ctx, sub.data(), (int32_t)sub.size(), scmos,
-                                                    tile, m.bufs[fam][c], &st);
-            if (st != GMLE_OK) return st;
-            if (tiles == 0) continue;
-            plan.tiles[fam][c] = tiles;
-            plan.smem[fam][c] = mixed_smem(sub.data(), (int32_t)sub.size(), scmos, tile);
-            plan.grid[fam][c] = mixed_grid(ctx, scmos, c, plan.smem[fam][c]);
+    std::vector<int> by_kind[kKinds];
+    int64_t rois[kKinds] = {};
+    for (int k = 0; k < ngroups; k++) {
+        const gmle_group &G = groups[k];
+        if (G.n <= 0) continue;
+        if (opt.allow_plain && G.n >= kPlainGroupRois) {
+            plan.plain.push_back(G);
+            continue;
         }
+        const int kind = kind_of(G.desc);
+        by_kind[kind].push_back(k);
+        rois[kind] += G.n;
+    }
+    for (int kind = 0; kind < kKinds; kind++) {
+        if (by_kind[kind].empty()) continue;
+        const gmle_fit_desc &d0 = groups[by_kind[kind][0]].desc;
+        TableLaunch L;
+        L.kind = kind;
+        L.model = d0.model;
+        L.box = d0.box;
+        L.scmos = d0.camera != GMLE_CAMERA_POISSON;
+        const Tuning t = pick_tuning(ctx, &d0, opt.shape_rois > 0 ? opt.shape_rois : rois[kind]);
+        const int rpb = t.rois_per_block;
+        int64_t tiles = 0;
+        for (int k : by_kind[kind]) tiles += (groups[k].n + rpb - 1) / rpb;
+        TableBufs &b = m.tables[kind];
+        st = ensure_table(ctx, b, std::max<int64_t>((int64_t)by_kind[kind].size(), opt.reserve_groups),
+                          std::max<int64_t>(tiles, opt.reserve_rois / rpb + opt.reserve_groups));
+        if (st != GMLE_OK) return st;
+        if (!m.zero_copy) CK(cudaEventSynchronize(b.reuse), "cudaEventSynchronize");
+        int64_t *hdr = reinterpret_cast<int64_t *>(b.h_base);
+        KernelArgs *args = reinterpret_cast<KernelArgs *>(b.h_base + kTableHeader);
+        int64_t *map = reinterpret_cast<int64_t *>(b.h_base + b.tiles_off());
+        int64_t tile = 0;
+        for (size_t q = 0; q < by_kind[kind].size(); q++) {
+            const gmle_group &G = groups[by_kind[kind][q]];
+            args[q] = make_args(ctx, &G.desc, G.data, G.x_corners, G.y_corners, G.n, G.params,
+                                G.crlb, G.llr, G.flags, t.tpr);
+            const int64_t nt = (G.n + rpb - 1) / rpb;
+            for (int64_t j = 0; j < nt; j++) map[tile + j] = ((int64_t)q << 32) | j;
+            tile += nt;
+        }
+        hdr[0] = (int64_t)by_kind[kind].size();
+        hdr[1] = tiles;
+        const int bps = gmle::table_blocks_per_sm(L.model, L.box, L.scmos, t.tpr, rpb);
+        if (bps <= 0)
+            return fail(ctx, GMLE_CUDA_ERROR, "no resident block for model %d box %d (tpr %d, %d ROIs)",
+                        L.model, L.box, t.tpr, rpb);
+        const int64_t full = (int64_t)ctx->num_sms * bps;
+        L.shape = gmle::LaunchShape{t.tpr, rpb, opt.full_grid ? full : std::min(full, tiles)};
+        L.groups = hdr[0];
+        L.tiles = tiles;
+        plan.launches.push_back(L);
     }
     return GMLE_OK;
 }
@@ -780,52 +720,60 @@ gmle_status upload_plan(gmle_ctx *ctx, MixedSet &m, const MixedPlan &plan, cudaS
                         bool record_reuse)
 {
     if (m.zero_copy) return GMLE_OK;
-    for (int fam = 0; fam < 2; fam++)
-        for (int c = 0; c < kClasses; c++) {
-            if (plan.tiles[fam][c] == 0) continue;
-            MixedBufs &b = m.bufs[fam][c];
-            const size_t bytes = kTableHeader + sizeof(gmle::GroupDesc) * (size_t)b.h_header[0];
-            CK(cudaMemcpyAsync(b.d_base, b.h_base, bytes, cudaMemcpyHostToDevice, s),
-               "H2D group table");
-            if (record_reuse) CK(cudaEventRecord(b.reuse, s), "cudaEventRecord");
-        }
+    for (const TableLaunch &L : plan.launches) {
+        TableBufs &b = m.tables[L.kind];
+        // the device table is rewritten after the last launch that read it
+        CK(cudaStreamWaitEvent(s, b.used, 0), "cudaStreamWaitEvent");
+        CK(cudaMemcpyAsync(b.d_base, b.h_base, kTableHeader + sizeof(KernelArgs) * L.groups,
+                           cudaMemcpyHostToDevice, s), "H2D group table");
+        CK(cudaMemcpyAsync(b.d_base + b.tiles_off(), b.h_base + b.tiles_off(),
+                           sizeof(int64_t) * L.tiles, cudaMemcpyHostToDevice, s), "H2D tile map");
+        if (record_reuse) CK(cudaEventRecord(b.reuse, s), "cudaEventRecord");
+    }
     return GMLE_OK;
 }
 
 gmle_status enqueue_plan(gmle_ctx *ctx, MixedSet &m, const MixedPlan &plan, cudaStream_t s)
 {
+    // Table launches of different kinds run concurrently with each other and
+    // with the plain launches (on the fork streams, joined back into s): each
+    // persistent grid's tail overlaps the next launch.
+    const int nl = (int)plan.launches.size();
+    const bool fork = nl > 1 || (nl == 1 && !plan.plain.empty());
+    const int nf = fork ? std::min(nl, kForks) : 0;
+    if (fork) {
+        CK(cudaEventRecord(m.ev_fork, s), "cudaEventRecord");
+        for (int f = 0; f < nf; f++)
+            CK(cudaStreamWaitEvent(m.fork[f], m.ev_fork, 0), "cudaStreamWaitEvent");
+    }
     for (const gmle_group &G : plan.plain) {
         const Tuning t = pick_tuning(ctx, &G.desc, G.n);
         KernelArgs a = make_args(ctx, &G.desc, G.data, G.x_corners, G.y_corners, G.n, G.params,
                                  G.crlb, G.llr, G.flags, t.tpr);
         CK(launch(ctx, &G.desc, a, t.rois_per_block, s), "fit kernel launch");
     }
-    // The persistent launches of different classes run concurrently (on the
-    // fork streams, joined back into s): small steps of the serving loop
-    // would otherwise leave the GPU idle in each launch's tail.
-    int used = 0;
-    for (int fam = 0; fam < 2; fam++)
-        for (int c = 0; c < kClasses; c++) used += plan.tiles[fam][c] > 0;
-    if (used > 1) CK(cudaEventRecord(m.ev_fork, s), "cudaEventRecord");
-    for (int c = 0; c < kClasses; c++) {
-        cudaStream_t q = s;
-        bool forked = false;
-        for (int fam = 0; fam < 2; fam++) {
-            if (plan.tiles[fam][c] == 0) continue;
-            if (used > 1 && !forked) {
-                q = m.fork[c];
-                CK(cudaStreamWaitEvent(q, m.ev_fork, 0), "cudaStreamWaitEvent");
-                forked = true;
-            }
-            ctx->launches++;
-            gmle_status st = enqueue_mixed(ctx, fam == 1, c, m.bufs[fam][c], plan.smem[fam][c],
-                                           plan.grid[fam][c], q, m.zero_copy);
-            if (st != GMLE_OK) return st;
-        }
-        if (forked) {
-            CK(cudaEventRecord(m.ev_join[c], q), "cudaEventRecord");
-            CK(cudaStreamWaitEvent(s, m.ev_join[c], 0), "cudaStreamWaitEvent");
-        }
+    for (int l = 0; l < nl; l++) {
+        const TableLaunch &L = plan.launches[l];
+        TableBufs &b = m.tables[L.kind];
+        cudaStream_t q = fork ? m.fork[l % nf] : s;
+        const char *base = m.zero_copy ? b.h_base : b.d_base;
+        gmle::TileTable t;
+        t.header = reinterpret_cast<const int64_t *>(base);
+        t.groups = reinterpret_cast<const KernelArgs *>(base + kTableHeader);
+        t.tiles = reinterpret_cast<const int64_t *>(base + b.tiles_off());
+        t.tile0 = nullptr;
+        t.counter = b.d_counter;
+        KernelArgs a;
+        std::memset(&a, 0, sizeof a);
+        a.tpr = L.shape.tpr;
+        CK(cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned long long), q), "reset tile counter");
+        ctx->launches++;
+        CK(gmle::launch_fit(L.model, L.box, L.scmos, a, t, L.shape, q), "table launch");
+        if (!m.zero_copy) CK(cudaEventRecord(b.used, q), "cudaEventRecord");
+    }
+    for (int f = 0; f < nf; f++) {
+        CK(cudaEventRecord(m.ev_join[f], m.fork[f]), "cudaEventRecord");
+        CK(cudaStreamWaitEvent(s, m.ev_join[f], 0), "cudaStreamWaitEvent");
     }
     return GMLE_OK;
 }
@@ -843,7 +791,7 @@ extern "C" gmle_status gmle_fit_mixed_device(gmle_ctx *ctx, const gmle_group *gr
     gmle_status st = init_mixed_set(ctx, ctx->mixed);
     if (st != GMLE_OK) return st;
     MixedPlan plan;
-    st = plan_mixed(ctx, groups, ngroups, ctx->mixed, plan, true);
+    st = plan_mixed(ctx, groups, ngroups, ctx->mixed, plan, PlanOptions());
     if (st != GMLE_OK) return st;
     st = upload_plan(ctx, ctx->mixed, plan, (cudaStream_t)stream, true);
     if (st != GMLE_OK) return st;

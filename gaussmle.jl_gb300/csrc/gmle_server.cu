@@ -6,10 +6,10 @@
 //   admit   -> arena allocation (device memory budget), ROIs and corners copied
 //              in on the input stream                        (admission by HBM)
 //   step    -> every admitted request whose copy has landed joins the next
-//              persistent mixed-batch launch; up to max_inflight_steps launches
-//              run concurrently on their own streams, each launch a replay of
-//              a CUDA graph captured once per (slot, camera family, shared-
-//              memory size)                                 (continuous batching)
+//              step: one persistent table launch per (camera family, model,
+//              box) present; up to max_inflight_steps steps run concurrently
+//              on their own streams, each step a replay of a CUDA graph
+//              captured once per (slot, launch pattern)    (continuous batching)
 //   drain   -> results copied out on the output stream, memory released,
 //              waiters woken; the latency submit -> results-on-host recorded.
 // The scheduler never waits on the GPU: it polls events and sleeps briefly when
@@ -17,7 +17,6 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <array>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -36,7 +35,7 @@ namespace {
 using Clock = std::chrono::steady_clock;
 
 constexpr int kMaxSlots = 8;
-constexpr int kServerTableCap = 4096;  // groups (requests) per launch and family
+constexpr int kServerTableCap = 4096;  // groups (requests) per step and kind
 
 enum ReqState { PENDING, STAGED, RUNNING, DRAINING, DONE, FAILED };
 
@@ -120,7 +119,7 @@ struct Server {
     cudaEvent_t step_done[kMaxSlots] = {};
     bool slot_busy[kMaxSlots] = {};
     MixedSet sets[kMaxSlots];
-    std::map<std::array<size_t, 2 * kClasses>, cudaGraphExec_t> graphs[kMaxSlots];
+    std::map<std::vector<int64_t>, cudaGraphExec_t> graphs[kMaxSlots];
     // statistics
     int64_t submitted = 0, completed = 0, rejected = 0, failed = 0, rois_done = 0, steps = 0;
     std::vector<float> lat_ms;
@@ -220,9 +219,11 @@ struct Server {
         return e;
     }
 
-    // One step: the tables of every (family, class) in the slot's pinned
-    // buffers, then a replay of the slot's graph for this launch pattern
-    // (captured on first use) or a direct enqueue.
+    // One step: the tables of every kind in the slot's pinned buffers (read
+    // in place by the kernels), then a replay of the slot's graph for this
+    // launch pattern (captured on first use) or a direct enqueue.  Shapes come
+    // from the tuning for a full step and grids are full, so the pattern only
+    // changes with the kinds present (or a new tuning or table).
     gmle_status launch_step(int slot, const std::vector<Request *> &reqs)
     {
         std::vector<gmle_group> groups;
@@ -232,20 +233,25 @@ struct Server {
         MixedPlan plan;
         {
             std::lock_guard<std::mutex> lk(ctx->mu);
-            gmle_status st = plan_mixed(ctx, groups.data(), (int32_t)groups.size(), m, plan,
-                                        false);
-            if (st != GMLE_OK) return st;
-            // zero-copy tables: nothing to upload; the graph holds the launches
-            st = upload_plan(ctx, m, plan, s_step[slot], false);
+            PlanOptions opt;
+            opt.allow_plain = false;
+            opt.shape_rois = cfg.max_step_rois;
+            opt.full_grid = true;
+            opt.reserve_groups = kServerTableCap;
+            opt.reserve_rois = cfg.max_step_rois;
+            gmle_status st = plan_mixed(ctx, groups.data(), (int32_t)groups.size(), m, plan, opt);
             if (st != GMLE_OK) return st;
             if (!cfg.use_graphs) {
                 st = enqueue_plan(ctx, m, plan, s_step[slot]);
                 if (st != GMLE_OK) return st;
             } else {
-                std::array<size_t, 2 * kClasses> key{};
-                for (int f = 0; f < 2; f++)
-                    for (int c = 0; c < kClasses; c++)
-                        key[f * kClasses + c] = plan.tiles[f][c] ? plan.smem[f][c] : 0;
+                std::vector<int64_t> key;
+                for (const TableLaunch &L : plan.launches) {
+                    const TableBufs &b = m.tables[L.kind];
+                    key.insert(key.end(), {L.kind, L.shape.tpr, L.shape.rois_per_block,
+                                           L.shape.grid, (int64_t)(uintptr_t)b.h_base,
+                                           b.cap_groups});
+                }
                 auto it = graphs[slot].find(key);
                 if (it == graphs[slot].end()) {
                     cudaGraph_t g = nullptr;
@@ -265,8 +271,7 @@ struct Server {
                     it = graphs[slot].emplace(key, ge).first;
                 } else {
                     // a replay launches the same kernels as the capture
-                    for (int f = 0; f < 2; f++)
-                        for (int c = 0; c < kClasses; c++) ctx->launches += plan.tiles[f][c] > 0;
+                    ctx->launches += (int64_t)plan.launches.size();
                 }
                 GMLE_CK(cudaGraphLaunch(it->second, s_step[slot]), "cudaGraphLaunch");
             }
@@ -482,14 +487,6 @@ gmle_status gmle_server_start(gmle_ctx *ctx, const gmle_server_config *config)
              cudaEventCreateWithFlags(&S->step_done[k], cudaEventDisableTiming) == cudaSuccess;
         ok = ok && init_mixed_set(ctx, S->sets[k]) == GMLE_OK;
         S->sets[k].zero_copy = true;
-        for (int f = 0; ok && f < 2; f++)
-            for (int c = 0; ok && c < kClasses; c++)
-                ok = ensure_mixed(ctx, S->sets[k].bufs[f][c], kServerTableCap) == GMLE_OK;
-    }
-    // set the kernels' shared-memory attribute outside any graph capture
-    for (int c = 0; c < kClasses; c++) {
-        gmle::mixed_blocks_per_sm(false, c, 48 * 1024);
-        gmle::mixed_blocks_per_sm(true, c, 48 * 1024);
     }
     ctx->server = S;
     if (!ok) {

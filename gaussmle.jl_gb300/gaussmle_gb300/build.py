@@ -1,8 +1,8 @@
 """Build libgaussmle_sm100a.so in-tree with nvcc for sm_103a.
 
-The library is the product: four per-model kernel translation units plus the
-C-ABI runtime, compiled in parallel (one -gencode, no cmake) and linked into
-``<package root>/lib/libgaussmle_sm100a.so``.
+The library is the product: eight kernel translation units (PSF model x camera
+family) plus the C-ABI runtime, compiled in parallel (one -gencode, no cmake;
+the heaviest units first) and linked into ``<package root>/lib/libgaussmle_sm100a.so``.
 """
 from __future__ import annotations
 
@@ -23,9 +23,9 @@ LIB_PATH = LIB_DIR / LIB_NAME
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2",
               f"-I{REPO_ROOT / 'include'}"]
-SOURCES = ["gmle_fit_xynb.cu", "gmle_fit_xynbs.cu", "gmle_fit_xynbsxsy.cu",
-           "gmle_fit_astig.cu", "gmle_mixed_poisson.cu", "gmle_mixed_scmos.cu",
-           "gmle_runtime.cu", "gmle_server.cu", "gmle_noalloc.cu"]
+SOURCES = [f"gmle_fit_{m}_{cam}.cu" for m in ("astig", "xynbsxsy", "xynbs", "xynb")
+           for cam in ("poisson", "scmos")] + ["gmle_runtime.cu", "gmle_server.cu",
+                                                "gmle_noalloc.cu"]
 
 
 def nvcc() -> str:

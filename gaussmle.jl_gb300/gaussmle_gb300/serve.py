@@ -42,7 +42,8 @@ def make_group(psf_pixels: PSFModel, box: int, camera: int, constraints: Paramet
 
 
 def fit_mixed_device(ctx: _lib.Context, groups: list[_lib.Group], stream=None) -> None:
-    """One persistent launch per camera family over all groups (device buffers)."""
+    """Fit device-resident groups: one persistent table launch per (camera family,
+    model, box) present, plain launches for groups of 65536 ROIs or more."""
     import torch
     arr = (_lib.Group * len(groups))(*groups)
     s = stream if stream is not None else torch.cuda.current_stream()

@@ -195,9 +195,11 @@ typedef struct {
 
 /*
  * Fit a mixed batch (any mix of PSF models and box sizes 5..15) of
- * device-resident groups with one persistent, work-stealing kernel launch per
- * camera family present, enqueued on `stream` (used as given).  No reference
- * counterpart: the reference fits one (model, box) per fit() call
+ * device-resident groups, enqueued on `stream` (used as given).  The groups of
+ * each (camera family, model, box) present share one persistent,
+ * work-stealing launch of that model's kernel; these launches run
+ * concurrently.  A group of 65536 ROIs or more gets its own plain launch.  No
+ * reference counterpart: the reference fits one (model, box) per fit() call
  * (src/interface.jl:177-291).
  */
 gmle_status gmle_fit_mixed_device(gmle_ctx *ctx, const gmle_group *groups, int32_t ngroups,
@@ -210,15 +212,16 @@ gmle_status gmle_fit_mixed_device(gmle_ctx *ctx, const gmle_group *groups, int32
  *
  * The call allocates nothing: no cudaMalloc, cudaFree, pinned memory, stream,
  * event or host heap, and it needs no context.  Its scratch is a static device
- * array of GMLE_NOALLOC_SCRATCH_BYTES (197,120 bytes).  The array holds the
- * persistent kernels' group tables, their work-stealing tile counters and a
+ * array of GMLE_NOALLOC_SCRATCH_BYTES (239,104 bytes).  The array holds the
+ * persistent launches' group tables, their work-stealing tile counters and a
  * skipped-ROI counter.  It is reserved on each GPU that loads the library's
  * device code and stays there until the process exits.
  *
  * groups    Device pointers, as for gmle_fit_mixed_device.  At most
  *           GMLE_NOALLOC_MAX_GROUPS groups; a larger ngroups returns
  *           GMLE_INVALID_ARG and launches nothing.  Every group runs in the
- *           persistent kernels, including groups of 65536 ROIs or more.
+ *           persistent launches, including groups of 65536 ROIs or more,
+ *           with the size-based default launch shapes.
  * variance, gain, offset
  *           Device (ny, nx) column-major calibration maps.  NULL when the
  *           batch is Poisson-only; gain and offset are needed for
@@ -228,8 +231,8 @@ gmle_status gmle_fit_mixed_device(gmle_ctx *ctx, const gmle_group *groups, int32
  * err       May be NULL.  Receives a failure's message, up to err_len bytes.
  *
  * Set-up: the first call on a device looks up the scratch address
- * (cudaGetSymbolAddress) and sets the kernels' attributes.  Make that first
- * call before any stream capture.
+ * (cudaGetSymbolAddress); the first launch of each kernel on a device sets its
+ * shared-memory limit.  Make that first call before any stream capture.
  *
  * Zeroing: the tile counters must be zero when each launch starts.  Every
  * call copies its tables into the scratch with one host-to-device copy on
@@ -240,7 +243,7 @@ gmle_status gmle_fit_mixed_device(gmle_ctx *ctx, const gmle_group *groups, int32
  * with no event ordering them.  Calls on one stream run in order.
  */
 #define GMLE_NOALLOC_MAX_GROUPS 1024
-#define GMLE_NOALLOC_SCRATCH_BYTES (512 + 192 * GMLE_NOALLOC_MAX_GROUPS)
+#define GMLE_NOALLOC_SCRATCH_BYTES (1536 + (8 + 224) * GMLE_NOALLOC_MAX_GROUPS)
 gmle_status gmle_fit_mixed_device_noalloc(const gmle_group *groups, int32_t ngroups,
                                           const float *variance, const float *gain,
                                           const float *offset, int32_t ny, int32_t nx,

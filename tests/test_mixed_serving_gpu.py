@@ -1,7 +1,8 @@
 """GPU tests of the mixed-batch persistent kernel and the serving loop.
 
-* One persistent launch over a heterogeneous batch gives the same results as
-  the plain kernel on each group alone (same arithmetic: bit-identical).
+* The persistent table launches of a heterogeneous batch give the same
+  results as the plain kernel on each group alone (same arithmetic and launch
+  shape: bit-identical), also for hundreds of small groups in one launch.
 * Served requests give the same result alone and in a mix, and match the
   FP32 oracle within the parity bar (tests/parity_cases.py).
 * Admission: a request that can never fit the HBM budget is rejected;
@@ -61,6 +62,11 @@ def _dev(torch, w):
     return t
 
 
+# Launch shapes forced per kind so that the table launch and the plain launch
+# run the same code: both kernels (one and several threads per ROI) are covered.
+SHAPES = [(1, 32), (2, 64), (4, 32), (1, 64), (8, 16)]
+
+
 def test_mixed_launch_matches_plain_kernel(ctx):
     torch = pytest.importorskip("torch")
     ws = _cases()
@@ -69,23 +75,61 @@ def test_mixed_launch_matches_plain_kernel(ctx):
     groups = [serve.make_group(w.psf, w.box, 2, w.constraints, b["data"], b["xc"], b["yc"],
                                b["params"], b["crlb"], b["llr"], b["flags"])
               for w, b in zip(ws, bufs)]
-    l0 = ctx.launches()
-    serve.fit_mixed_device(ctx, groups)
-    torch.cuda.synchronize()
-    # one persistent launch per shared-memory class present (boxes <= 9, 11, >= 13)
-    assert ctx.launches() - l0 == 3
-    for w, b in zip(ws, bufs):
-        ref = _dev(torch, w)
-        ctx.check(ctx.lib.gmle_set_tuning(ctx.handle, w.psf.model_id, w.box, 2, 1, 32))
-        try:
+    try:
+        for w, (tpr, rpb) in zip(ws, SHAPES):
+            ctx.check(ctx.lib.gmle_set_tuning(ctx.handle, w.psf.model_id, w.box, 2, tpr, rpb))
+        l0 = ctx.launches()
+        serve.fit_mixed_device(ctx, groups)
+        torch.cuda.synchronize()
+        # one persistent table launch per (camera family, model, box) present
+        assert ctx.launches() - l0 == len(ws)
+        for w, b in zip(ws, bufs):
+            ref = _dev(torch, w)
             G.fit_device(ctx, make_desc(w.psf, w.box, 20, w.constraints, 2), ref["data"],
                          ref["xc"], ref["yc"], ref["params"], ref["crlb"], ref["llr"], ref["flags"])
             torch.cuda.synchronize()
-        finally:
+            for k in ("params", "crlb", "llr", "flags"):
+                a, r = b[k].cpu().numpy(), ref[k].cpu().numpy()
+                assert np.array_equal(a, r, equal_nan=True), (w.name, k, np.nanmax(np.abs(a - r)))
+    finally:
+        for w in ws:
             ctx.check(ctx.lib.gmle_set_tuning(ctx.handle, w.psf.model_id, w.box, 2, 0, 0))
-        for k in ("params", "crlb", "llr", "flags"):
-            a, r = b[k].cpu().numpy(), ref[k].cpu().numpy()
-            assert np.array_equal(a, r, equal_nan=True), (w.name, k, np.nanmax(np.abs(a - r)))
+
+
+def test_table_launch_takes_many_small_groups(ctx):
+    """Hundreds of small groups of one kind share a launch: every ROI is fitted
+    once, with the result of the plain kernel on the whole batch."""
+    torch = pytest.importorskip("torch")
+    w = make_case("xynb-9-poisson", 0, 9, 0, 5000, seed=21)
+    dev = torch.device("cuda", 0)
+    data = torch.from_numpy(np.ascontiguousarray(w.data.transpose(2, 1, 0)).reshape(-1)).to(dev)
+    desc = make_desc(w.psf, 9, 20, w.constraints, 0)
+    ref = {"params": torch.empty((5000, 4), device=dev), "crlb": torch.empty((5000, 4), device=dev),
+           "llr": torch.empty(5000, device=dev), "flags": torch.empty(5000, dtype=torch.uint8,
+                                                                        device=dev)}
+    out = {k: torch.full_like(v, float("nan")) if v.dtype != torch.uint8 else torch.zeros_like(v)
+           for k, v in ref.items()}
+    try:
+        ctx.check(ctx.lib.gmle_set_tuning(ctx.handle, 0, 9, 0, 1, 32))
+        G.fit_device(ctx, desc, data, None, None, ref["params"], ref["crlb"], ref["llr"],
+                     ref["flags"])
+        # ragged groups of 1..40 ROIs
+        rng = np.random.default_rng(3)
+        cuts = np.cumsum(rng.integers(1, 41, 400))
+        cuts = np.concatenate([[0], cuts[cuts < 5000], [5000]])
+        groups = []
+        for lo, hi in zip(cuts[:-1], cuts[1:]):
+            groups.append(serve.make_group(
+                w.psf, 9, 0, w.constraints, data[lo * 81:hi * 81], None, None,
+                out["params"][lo:hi], out["crlb"][lo:hi], out["llr"][lo:hi], out["flags"][lo:hi]))
+        l0 = ctx.launches()
+        serve.fit_mixed_device(ctx, groups)
+        torch.cuda.synchronize()
+        assert ctx.launches() - l0 == 1
+        for k in ref:
+            assert np.array_equal(out[k].cpu().numpy(), ref[k].cpu().numpy(), equal_nan=True), k
+    finally:
+        ctx.check(ctx.lib.gmle_set_tuning(ctx.handle, 0, 9, 0, 0, 0))
 
 
 def _host_bufs(w):

@@ -1,8 +1,8 @@
 """gmle_fit_mixed_device_noalloc: the mixed-batch fit whose scratch is the
 library's static device array, called through the C ABI.
 
-The GPU test fits one heterogeneous batch, spanning both camera families and all
-three shared-memory classes, with the context entry point gmle_fit_mixed_device.
+The GPU test fits one heterogeneous batch, spanning both camera families and
+several models and box sizes, with the context entry point gmle_fit_mixed_device.
 It then makes two calls in a row of the no-allocation entry point on one
 stream, each into fresh NaN-filled outputs.  Both calls must match the
 context path within the parity tolerances.  No device memory may be taken
