@@ -52,7 +52,12 @@ WORKLOAD = ("mixed-batch: 40% XYNB 11x11, 25% XYNBS 9x9, 15% XYNBSXSY 13x13, "
 # DRAM bytes (read + write) per ROI of a launch, from one ncu capture of the
 # kernel (dram__bytes_read.sum + dram__bytes_write.sum over the ROIs of the
 # captured launch); the roofline's traffic scales it to the timed launch.
-TRAFFIC_BYTES_PER_ROI: dict[str, float] = {}
+TRAFFIC_BYTES_PER_ROI: dict[str, float] = {
+    # 90 000 ROIs, 4 threads per ROI, 32 ROIs/block: 150.3 MB read + 5.8 MB written
+    "fit_kernel<3, 15, true, false>": 1734.7,
+    # 240 000 ROIs, one thread per ROI, 32 ROIs/block: 200.7 MB read + 10.3 MB written
+    "fit_kernel_r1<0, 11, true, false>": 879.2,
+}
 
 
 def parse():
@@ -68,8 +73,10 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-latency", action="store_true")
     p.add_argument("--no-extras", action="store_true")
-    p.add_argument("--loads", default="5e6,2e7",
+    p.add_argument("--loads", default="1e6,5e6,2e7,5e7",
                    help="offered loads (ROIs/s) of the latency measurement")
+    p.add_argument("--loads-10k", default="2e7,5e7",
+                   help="offered loads (ROIs/s) of the 10 000-ROI request latency measurement")
     p.add_argument("--load-rois", type=float, default=2e7,
                    help="ROIs of arrivals per load point (bounded to about 1.5 s)")
     return p.parse_args()
@@ -268,7 +275,7 @@ def time_steps(torch, stream, fn, steps, warmup):
     return e0.elapsed_time(e1) / 1e3
 
 
-def extras(torch, ctx, dev, steps):
+def extras(torch, ctx, dev, steps, peak_inst):
     """Plain-kernel throughput of the other workloads (device-resident)."""
     import gaussmle_gb300 as G
     from gaussmle_gb300 import simulate, roofline
@@ -298,7 +305,8 @@ def extras(torch, ctx, dev, steps):
         per = dt / steps
         w = roofline.work_per_roi(model, box, 20, cam)
         out[name] = {"fits_per_s": n / per, "ms_per_launch": per * 1e3,
-                     "shape": [tpr, rpb], "work_fp32_equiv_per_roi": w["fp32_equiv"]}
+                     "shape": [tpr, rpb], "work_fp32_equiv_per_roi": w["fp32_equiv"],
+                     "roofline_frac": n * w["fp32_equiv"] / per / 1e12 / peak_inst}
         del wl, prm, crl, llr, flg
         torch.cuda.empty_cache()
     return out
@@ -345,11 +353,13 @@ def run_ours(args):
         dist.barrier()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("value")  # the timed region, for profiler filters
     e0.record(stream)
     for _ in range(args.steps):
         step()
     e1.record(stream)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     clocks = sampler.stop()
     dt = e0.elapsed_time(e1) / 1e3
     if world > 1:
@@ -364,11 +374,13 @@ def run_ours(args):
 
     # ---- each group's launch alone: the dominant kernel and its roofline ----
     per_group = []
+    torch.cuda.nvtx.range_push("per_group")
     for g, b in zip(groups, dgs):
         fn = (lambda g=g, b=b: G.fit_device(ctx, b["group"].desc, g["data"], g["xc"], g["yc"],
                                              b["params"], b["crlb"], b["llr"], b["flags"],
                                              stream=stream))
         per_group.append(time_steps(torch, stream, fn, args.steps, 3) / args.steps)
+    torch.cuda.nvtx.range_pop()
     dt_plain_dev = sum(per_group) * args.steps
 
     # ---- the same batch as requests of <= 50000 ROIs: table launches only ----
@@ -426,12 +438,18 @@ def run_ours(args):
                          "one_launch_per_group_device": {"value": n * args.steps / dt_plain_dev,
                                                          "unit": UNIT}}
             if not args.no_latency:
-                latency = {"served": [], "plain": []}
+                latency = {"served": [], "plain": [], "served_10k": [], "plain_10k": []}
                 for load in [float(x) for x in args.loads.split(",")]:
                     tot = min(args.load_rois, load * 1.5)
                     lreqs = loadgen.make_stream(pools, int(tot), seed=13)
                     latency["served"].append(loadgen.run_stream_served(srv, pools, lreqs, load))
                     latency["plain"].append(loadgen.run_stream_plain(ctx, pools, lreqs, load))
+                # requests of exactly 10 000 ROIs (the p99 < 10 ms target's request size)
+                for load in [float(x) for x in args.loads_10k.split(",")]:
+                    tot = min(args.load_rois, load * 1.5)
+                    lreqs = loadgen.make_stream(pools, int(tot), seed=17, lo=10_000, hi=10_000)
+                    latency["served_10k"].append(loadgen.run_stream_served(srv, pools, lreqs, load))
+                    latency["plain_10k"].append(loadgen.run_stream_plain(ctx, pools, lreqs, load))
         finally:
             srv.stop()
 
@@ -474,7 +492,7 @@ def run_ours(args):
     if not args.no_extras and world == 1:
         del dgs
         torch.cuda.empty_cache()
-        ext = extras(torch, ctx, dev, max(3, args.steps // 2))
+        ext = extras(torch, ctx, dev, max(3, args.steps // 2), peak_inst)
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True,

@@ -69,14 +69,15 @@ class HostPools:
 
 def make_stream(pools: HostPools, total_rois: int, seed: int = 7, lo: int = 50,
                 hi: int = 50000) -> list[Request]:
-    """Requests until total_rois: sizes log-uniform [lo, hi], groups by the
-    mix proportions, ROI slices taken round-robin from each group's pool."""
+    """Requests until total_rois: sizes log-uniform [lo, hi] (all `lo` when
+    lo == hi), groups by the mix proportions, ROI slices taken round-robin
+    from each group's pool."""
     rng = np.random.default_rng(seed)
     cursor = [0] * len(pools.g)
     out, tot = [], 0
     while tot < total_rois:
         gi = int(rng.choice(len(pools.g), p=pools.p))
-        n = int(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        n = lo if lo == hi else int(np.exp(rng.uniform(np.log(lo), np.log(hi))))
         cap = pools.g[gi]["n"]
         n = min(n, cap)
         if cursor[gi] + n > cap:
