@@ -20,8 +20,9 @@
 //  * Gradient and diagonal Hessian are summed with warp shuffles; every lane
 //    of the group then applies the same Newton step, so theta stays identical.
 //  * Final pass: FP32 per-pixel Fisher products, summed per column in FP32
-//    (<= 15 terms) and across columns and lanes in FP64; Cholesky (LU
-//    fallback) inversion in FP64.
+//    (<= 15 terms) and across columns and lanes as a compensated double-float
+//    (FP64-class accuracy at FP32 cost); Cholesky (LU fallback) inversion in
+//    FP64.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -257,6 +258,49 @@ __device__ __forceinline__ double group_sum(double v, int tpr)
 {
     for (int off = tpr >> 1; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
     return v;
+}
+
+// ---- compensated (double-float) accumulation of the Fisher matrix ------------
+//
+// A value is an unevaluated sum hi + lo of two floats.  TwoSum (Moller 1965,
+// Knuth TAOCP vol. 2, 4.2.2) gives the exact rounding error of a float
+// addition in 6 additions, so the accumulated sum of FP32 terms is carried to
+// about 2^-48 relative, like an FP64 accumulator, at FP32 cost: FP64 runs at
+// 1/64 of the FP32 rate on GB300.  The sum becomes a double (hi + lo, exact)
+// for the FP64 inversion.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = __fadd_rn(a, b);
+    const float bb = __fadd_rn(s, -a);
+    e = __fadd_rn(__fadd_rn(a, -__fadd_rn(s, -bb)), __fadd_rn(b, -bb));
+}
+
+// hi + lo += x
+__device__ __forceinline__ void dd_add(float &hi, float &lo, float x)
+{
+    float s, e;
+    two_sum(hi, x, s, e);
+    hi = s;
+    lo = __fadd_rn(lo, e);
+}
+
+// (hi, lo) summed over the tpr lanes of a group (all lanes get the same sum:
+// TwoSum's error term is exact, so it does not depend on the operand order).
+__device__ __forceinline__ void dd_group_sum(float &hi, float &lo, int tpr)
+{
+    for (int off = tpr >> 1; off > 0; off >>= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, hi, off);
+        const float ol = __shfl_xor_sync(0xffffffffu, lo, off);
+        float s, e;
+        two_sum(hi, oh, s, e);
+        e = __fadd_rn(e, __fadd_rn(lo, ol));
+        two_sum(s, e, hi, lo);  // renormalise: |lo| <= ulp(hi) / 2
+    }
+}
+
+__device__ __forceinline__ double dd_to_double(float hi, float lo)
+{
+    return __dadd_rn((double)hi, (double)lo);
 }
 
 // ---- initialisation, src/unified_kernel.jl:158-255 (one lane, reference order,
@@ -751,11 +795,12 @@ __device__ __forceinline__ void final_pixel(float d, float v, float mu, float py
 }
 
 // One column's Fisher contribution: F_kl += sum_{t,u} a_kt a_lu Q[b_kt][b_lu],
-// summed in FP32 for the column and accumulated in FP64.
+// summed in FP32 for the column and accumulated across columns as a
+// double-float (Fh + Fl, upper triangle).
 template <int MODEL, int P, int NB>
-__device__ __forceinline__ void fisher_column(double (&Fm)[P][P], const float (&Q)[NB][NB],
-                                              float xp, float xd1, float xs1,
-                                              const AstigWidths &aw)
+__device__ __forceinline__ void fisher_column(float (&Fh)[P][P], float (&Fl)[P][P],
+                                              const float (&Q)[NB][NB], float xp, float xd1,
+                                              float xs1, const AstigWidths &aw)
 {
     using S = Slots<MODEL>;
     float av[P][2];
@@ -777,7 +822,7 @@ __device__ __forceinline__ void fisher_column(double (&Fm)[P][P], const float (&
                 for (int tl = 0; tl < term_count(MODEL, l); tl++)
                     s = fmaf(av[k][tk] * av[l][tl],
                              qsym<NB>(Q, term_b(MODEL, k, tk), term_b(MODEL, l, tl)), s);
-            Fm[k][l] += (double)s;
+            dd_add(Fh[k][l], Fl[k][l], s);
         }
 }
 
@@ -923,11 +968,11 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
             newton_step<P>(th, gs, hs, a);
         } else {
             float llr = 0.f;
-            double Fm[P][P];
+            float Fh[P][P], Fl[P][P];
 #pragma unroll
             for (int k = 0; k < P; k++)
 #pragma unroll
-                for (int l = 0; l < P; l++) Fm[k][l] = 0.0;
+                for (int l = 0; l < P; l++) { Fh[k][l] = 0.f; Fl[k][l] = 0.f; }
             for (int j = 1; j <= BOX; j++) {
                 float nxp, nxd1, nxd2, nxs1 = 0.f, nxs2 = 0.f;
                 walk_entry<SIG, false>(j + 1, ax, wx, nxp, nxd1, nxd2, nxs1, nxs2);
@@ -950,13 +995,17 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
                     const float mu = fmaf(npx, py[t], bg);
                     final_pixel<SCMOS, SIG, NB>(d, v, mu, py[t], yd1[t], SIG ? ys1[t] : 0.f, llr, Q);
                 }
-                fisher_column<MODEL, P, NB>(Fm, Q, xp, xd1, xs1, aw);
+                fisher_column<MODEL, P, NB>(Fh, Fl, Q, xp, xd1, xs1, aw);
                 xp = nxp; xd1 = nxd1; xs1 = nxs1;
             }
+            double Fm[P][P];
 #pragma unroll
             for (int k = 0; k < P; k++)
 #pragma unroll
-                for (int l = k + 1; l < P; l++) Fm[l][k] = Fm[k][l];
+                for (int l = k; l < P; l++) {
+                    Fm[k][l] = dd_to_double(Fh[k][l], Fl[k][l]);
+                    Fm[l][k] = Fm[k][l];
+                }
             if (g < nroi) write_result<P>(a, roi0 + g, valid, th, Fm, llr);
         }
     }
@@ -1123,11 +1172,11 @@ __device__ __forceinline__ void fit_rois_tpr(const KernelArgs &a, int64_t roi0, 
                 if (SIG) ys1r[t] = ytab[3 * BOX + t];
             }
             float llr = 0.f;
-            double Fm[P][P];
+            float Fh[P][P], Fl[P][P];
 #pragma unroll
             for (int k = 0; k < P; k++)
 #pragma unroll
-                for (int l = 0; l < P; l++) Fm[k][l] = 0.0;
+                for (int l = 0; l < P; l++) { Fh[k][l] = 0.f; Fl[k][l] = 0.f; }
             for (int j = b0 + 1; j <= b1; j++) {
                 float xp, xd1, xd2, xs1 = 0.f, xs2 = 0.f;
                 walk_entry<SIG, false>(j, ax, wx, xp, xd1, xd2, xs1, xs2);
@@ -1151,14 +1200,16 @@ __device__ __forceinline__ void fit_rois_tpr(const KernelArgs &a, int64_t roi0, 
                     final_pixel<SCMOS, SIG, NB>(d, v, mu, py[t], yd1r[t], SIG ? ys1r[t] : 0.f,
                                                 llr, Q);
                 }
-                fisher_column<MODEL, P, NB>(Fm, Q, xp, xd1, xs1, aw);
+                fisher_column<MODEL, P, NB>(Fh, Fl, Q, xp, xd1, xs1, aw);
             }
             llr = group_sum(llr, tpr);
+            double Fm[P][P];
 #pragma unroll
             for (int k = 0; k < P; k++)
 #pragma unroll
                 for (int l = k; l < P; l++) {
-                    Fm[k][l] = group_sum(Fm[k][l], tpr);
+                    dd_group_sum(Fh[k][l], Fl[k][l], tpr);
+                    Fm[k][l] = dd_to_double(Fh[k][l], Fl[k][l]);
                     Fm[l][k] = Fm[k][l];
                 }
             if (r == 0 && g < nroi) write_result<P>(a, roi0 + g, valid, th, Fm, llr);

@@ -1,5 +1,7 @@
 // gmle_noalloc.cu - gmle_fit_mixed_device_noalloc: the mixed-batch fit for
-// callers that cannot allocate device memory.
+// callers that cannot allocate device memory: hosts whose device memory is held
+// by their own pool allocator (CUDA.jl, PyTorch), and code where a cudaMalloc,
+// which can synchronise the device, must not happen.
 //
 // A mixed batch runs as one persistent table launch per (camera family, PSF
 // model, box size) present (gmle_fit_kernel.cuh, TileTable).  Those launches

@@ -210,6 +210,14 @@ gmle_status gmle_fit_mixed_device(gmle_ctx *ctx, const gmle_group *groups, int32
  * counterpart in the reference, which allocates its device arrays in every
  * fit() call (src/interface.jl:229-240, :341-349, :428-436).
  *
+ * Who needs it: a host process whose device memory is owned by its own pool
+ * allocator (CUDA.jl's memory pool, PyTorch's caching allocator) and that has
+ * reserved most of the GPU for it, so an allocation by the library can fail or
+ * break the pool's accounting.  Also code that must not call cudaMalloc
+ * because it can synchronise the whole device and stall other streams.  Such
+ * a caller brings its inputs and outputs in its own memory, and this call
+ * adds nothing to the process's device memory.
+ *
  * The call allocates nothing: no cudaMalloc, cudaFree, pinned memory, stream,
  * event or host heap, and it needs no context.  Its scratch is a static device
  * array of GMLE_NOALLOC_SCRATCH_BYTES (239,104 bytes).  The array holds the

@@ -1,6 +1,10 @@
 """gmle_fit_mixed_device_noalloc: the mixed-batch fit whose scratch is the
 library's static device array, called through the C ABI.
 
+It serves callers that cannot allocate device memory: a host whose GPU memory
+is held by its own pool allocator (CUDA.jl, PyTorch), or code where a
+cudaMalloc, which can synchronise the device, is not allowed.
+
 The GPU test fits one heterogeneous batch, spanning both camera families and
 several models and box sizes, with the context entry point gmle_fit_mixed_device.
 It then makes two calls in a row of the no-allocation entry point on one
