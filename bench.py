@@ -77,6 +77,10 @@ def parse():
                    help="offered loads (ROIs/s) of the latency measurement")
     p.add_argument("--loads-10k", default="2e7,5e7",
                    help="offered loads (ROIs/s) of the 10 000-ROI request latency measurement")
+    p.add_argument("--max-step-rois", type=int, default=0,
+                   help="serving loop: ROIs per step (0: the library default)")
+    p.add_argument("--max-inflight", type=int, default=0,
+                   help="serving loop: concurrent steps (0: the library default)")
     p.add_argument("--load-rois", type=float, default=2e7,
                    help="ROIs of arrivals per load point (bounded to about 1.5 s)")
     return p.parse_args()
@@ -413,7 +417,8 @@ def run_ours(args):
     if not args.no_e2e or not args.no_latency:
         pools = loadgen.HostPools(groups)
         reqs = loadgen.make_stream(pools, n, seed=7 + rank)
-        srv = serve.Server(ctx, max_inflight_steps=4)
+        srv = serve.Server(ctx, max_inflight_steps=args.max_inflight,
+                           max_step_rois=args.max_step_rois)
         try:
             if not args.no_e2e:
                 for _ in range(max(1, min(args.warmup, 2))):

@@ -154,6 +154,8 @@ gmle_status plan_mixed(gmle_ctx *ctx, const gmle_group *groups, int32_t ngroups,
 // record_reuse each table's reuse event is recorded after its copy.
 gmle_status upload_plan(gmle_ctx *ctx, MixedSet &m, const MixedPlan &plan, cudaStream_t s,
                         bool record_reuse);
+// One table launch of a plan on q: its tile counter reset, then the kernel.
+gmle_status enqueue_table_launch(gmle_ctx *ctx, MixedSet &m, const TableLaunch &L, cudaStream_t q);
 // The plan's plain launches on s, then its table launches, concurrently on
 // m.fork when there are several, joined back into s.
 gmle_status enqueue_plan(gmle_ctx *ctx, MixedSet &m, const MixedPlan &plan, cudaStream_t s);

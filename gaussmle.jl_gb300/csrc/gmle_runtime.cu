@@ -589,7 +589,8 @@ void free_table(TableBufs &b)
 }
 
 // Room for `groups` groups and `tiles` tiles (grown by half again when short).
-gmle_status ensure_table(gmle_ctx *ctx, TableBufs &b, int64_t groups, int64_t tiles)
+gmle_status ensure_table(gmle_ctx *ctx, TableBufs &b, int64_t groups, int64_t tiles,
+                         bool device_copy)
 {
     if (!b.reuse) {
         CK(cudaEventCreateWithFlags(&b.reuse, cudaEventDisableTiming), "cudaEventCreate");
@@ -605,7 +606,7 @@ gmle_status ensure_table(gmle_ctx *ctx, TableBufs &b, int64_t groups, int64_t ti
     b.cap_groups = std::max<int64_t>({64, groups, b.cap_groups + b.cap_groups / 2});
     b.cap_tiles = std::max<int64_t>({1024, tiles, b.cap_tiles + b.cap_tiles / 2});
     CK(cudaMallocHost(&b.h_base, b.bytes()), "cudaMallocHost(group table)");
-    CK(cudaMalloc(&b.d_base, b.bytes()), "cudaMalloc(group table)");
+    if (device_copy) CK(cudaMalloc(&b.d_base, b.bytes()), "cudaMalloc(group table)");
     return GMLE_OK;
 }
 
@@ -686,7 +687,8 @@ gmle_status plan_mixed(gmle_ctx *ctx, const gmle_group *groups, int32_t ngroups,
         for (int k : by_kind[kind]) tiles += (groups[k].n + rpb - 1) / rpb;
         TableBufs &b = m.tables[kind];
         st = ensure_table(ctx, b, std::max<int64_t>((int64_t)by_kind[kind].size(), opt.reserve_groups),
-                          std::max<int64_t>(tiles, opt.reserve_rois / rpb + opt.reserve_groups));
+                          std::max<int64_t>(tiles, opt.reserve_rois / rpb + opt.reserve_groups),
+                          !m.zero_copy);
         if (st != GMLE_OK) return st;
         if (!m.zero_copy) CK(cudaEventSynchronize(b.reuse), "cudaEventSynchronize");
         int64_t *hdr = reinterpret_cast<int64_t *>(b.h_base);
@@ -733,6 +735,26 @@ gmle_status upload_plan(gmle_ctx *ctx, MixedSet &m, const MixedPlan &plan, cudaS
     return GMLE_OK;
 }
 
+gmle_status enqueue_table_launch(gmle_ctx *ctx, MixedSet &m, const TableLaunch &L, cudaStream_t q)
+{
+    TableBufs &b = m.tables[L.kind];
+    const char *base = m.zero_copy ? b.h_base : b.d_base;
+    gmle::TileTable t;
+    t.header = reinterpret_cast<const int64_t *>(base);
+    t.groups = reinterpret_cast<const KernelArgs *>(base + kTableHeader);
+    t.tiles = reinterpret_cast<const int64_t *>(base + b.tiles_off());
+    t.tile0 = nullptr;
+    t.counter = b.d_counter;
+    KernelArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.tpr = L.shape.tpr;
+    CK(cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned long long), q), "reset tile counter");
+    ctx->launches++;
+    CK(gmle::launch_fit(L.model, L.box, L.scmos, a, t, L.shape, q), "table launch");
+    if (!m.zero_copy) CK(cudaEventRecord(b.used, q), "cudaEventRecord");
+    return GMLE_OK;
+}
+
 gmle_status enqueue_plan(gmle_ctx *ctx, MixedSet &m, const MixedPlan &plan, cudaStream_t s)
 {
     // Table launches of different kinds run concurrently with each other and
@@ -753,23 +775,9 @@ gmle_status enqueue_plan(gmle_ctx *ctx, MixedSet &m, const MixedPlan &plan, cuda
         CK(launch(ctx, &G.desc, a, t.rois_per_block, s), "fit kernel launch");
     }
     for (int l = 0; l < nl; l++) {
-        const TableLaunch &L = plan.launches[l];
-        TableBufs &b = m.tables[L.kind];
-        cudaStream_t q = fork ? m.fork[l % nf] : s;
-        const char *base = m.zero_copy ? b.h_base : b.d_base;
-        gmle::TileTable t;
-        t.header = reinterpret_cast<const int64_t *>(base);
-        t.groups = reinterpret_cast<const KernelArgs *>(base + kTableHeader);
-        t.tiles = reinterpret_cast<const int64_t *>(base + b.tiles_off());
-        t.tile0 = nullptr;
-        t.counter = b.d_counter;
-        KernelArgs a;
-        std::memset(&a, 0, sizeof a);
-        a.tpr = L.shape.tpr;
-        CK(cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned long long), q), "reset tile counter");
-        ctx->launches++;
-        CK(gmle::launch_fit(L.model, L.box, L.scmos, a, t, L.shape, q), "table launch");
-        if (!m.zero_copy) CK(cudaEventRecord(b.used, q), "cudaEventRecord");
+        const gmle_status st = enqueue_table_launch(ctx, m, plan.launches[l],
+                                                    fork ? m.fork[l % nf] : s);
+        if (st != GMLE_OK) return st;
     }
     for (int f = 0; f < nf; f++) {
         CK(cudaEventRecord(m.ev_join[f], m.fork[f]), "cudaEventRecord");

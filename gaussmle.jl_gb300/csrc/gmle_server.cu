@@ -8,8 +8,8 @@
 //   step    -> every admitted request whose copy has landed joins the next
 //              step: one persistent table launch per (camera family, model,
 //              box) present; up to max_inflight_steps steps run concurrently
-//              on their own streams, each step a replay of a CUDA graph
-//              captured once per (slot, launch pattern)    (continuous batching)
+//              on their own streams, each kind's launch a replay of a CUDA
+//              graph captured once per (slot, kind)        (continuous batching)
 //   drain   -> results copied out on the output stream, memory released,
 //              waiters woken; the latency submit -> results-on-host recorded.
 // The scheduler never waits on the GPU: it polls events and sleeps briefly when
@@ -119,7 +119,13 @@ struct Server {
     cudaEvent_t step_done[kMaxSlots] = {};
     bool slot_busy[kMaxSlots] = {};
     MixedSet sets[kMaxSlots];
-    std::map<std::vector<int64_t>, cudaGraphExec_t> graphs[kMaxSlots];
+    // per slot and kind: the captured counter reset + table launch, and the
+    // shape and table it was captured for
+    struct KindGraph {
+        std::vector<int64_t> key;
+        cudaGraphExec_t exec = nullptr;
+    };
+    KindGraph graphs[kMaxSlots][kKinds];
     // statistics
     int64_t submitted = 0, completed = 0, rejected = 0, failed = 0, rois_done = 0, steps = 0;
     std::vector<float> lat_ms;
@@ -220,10 +226,12 @@ struct Server {
     }
 
     // One step: the tables of every kind in the slot's pinned buffers (read
-    // in place by the kernels), then a replay of the slot's graph for this
-    // launch pattern (captured on first use) or a direct enqueue.  Shapes come
-    // from the tuning for a full step and grids are full, so the pattern only
-    // changes with the kinds present (or a new tuning or table).
+    // in place by the kernels), then per kind present a replay of the slot's
+    // graph for that kind (captured on first use, or again after its shape or
+    // table changed), the kinds concurrently on the slot's fork streams.
+    // Shapes come from the tuning for a full step and grids are full, so each
+    // (slot, kind) is captured once: no capture stalls the loop once every
+    // kind has been seen.
     gmle_status launch_step(int slot, const std::vector<Request *> &reqs)
     {
         std::vector<gmle_group> groups;
@@ -231,6 +239,7 @@ struct Server {
         for (Request *r : reqs) groups.push_back(r->dev);
         MixedSet &m = sets[slot];
         MixedPlan plan;
+        cudaStream_t s = s_step[slot];
         {
             std::lock_guard<std::mutex> lk(ctx->mu);
             PlanOptions opt;
@@ -242,41 +251,54 @@ struct Server {
             gmle_status st = plan_mixed(ctx, groups.data(), (int32_t)groups.size(), m, plan, opt);
             if (st != GMLE_OK) return st;
             if (!cfg.use_graphs) {
-                st = enqueue_plan(ctx, m, plan, s_step[slot]);
+                st = enqueue_plan(ctx, m, plan, s);
                 if (st != GMLE_OK) return st;
             } else {
-                std::vector<int64_t> key;
                 for (const TableLaunch &L : plan.launches) {
                     const TableBufs &b = m.tables[L.kind];
-                    key.insert(key.end(), {L.kind, L.shape.tpr, L.shape.rois_per_block,
-                                           L.shape.grid, (int64_t)(uintptr_t)b.h_base,
-                                           b.cap_groups});
-                }
-                auto it = graphs[slot].find(key);
-                if (it == graphs[slot].end()) {
+                    const std::vector<int64_t> key = {L.shape.tpr, L.shape.rois_per_block,
+                                                      L.shape.grid, (int64_t)(uintptr_t)b.h_base,
+                                                      b.cap_groups};
+                    KindGraph &kg = graphs[slot][L.kind];
+                    if (kg.exec && kg.key == key) continue;
+                    if (kg.exec) cudaGraphExecDestroy(kg.exec);
+                    kg.exec = nullptr;
                     cudaGraph_t g = nullptr;
-                    cudaGraphExec_t ge = nullptr;
-                    GMLE_CK(cudaStreamBeginCapture(s_step[slot], cudaStreamCaptureModeThreadLocal),
+                    GMLE_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal),
                             "cudaStreamBeginCapture");
-                    st = enqueue_plan(ctx, m, plan, s_step[slot]);
-                    const cudaError_t e = cudaStreamEndCapture(s_step[slot], &g);
+                    st = enqueue_table_launch(ctx, m, L, s);
+                    ctx->launches--;  // counted when the graph is launched
+                    const cudaError_t e = cudaStreamEndCapture(s, &g);
                     if (st != GMLE_OK) {
                         if (g) cudaGraphDestroy(g);
                         return st;
                     }
                     GMLE_CK(e, "cudaStreamEndCapture");
-                    const cudaError_t e2 = cudaGraphInstantiate(&ge, g, 0);
+                    const cudaError_t e2 = cudaGraphInstantiate(&kg.exec, g, 0);
                     cudaGraphDestroy(g);
                     GMLE_CK(e2, "cudaGraphInstantiate");
-                    it = graphs[slot].emplace(key, ge).first;
-                } else {
-                    // a replay launches the same kernels as the capture
-                    ctx->launches += (int64_t)plan.launches.size();
+                    kg.key = key;
                 }
-                GMLE_CK(cudaGraphLaunch(it->second, s_step[slot]), "cudaGraphLaunch");
+                const int nl = (int)plan.launches.size();
+                const int nf = std::min(nl, kForks);
+                if (nl > 1) {
+                    GMLE_CK(cudaEventRecord(m.ev_fork, s), "cudaEventRecord");
+                    for (int f = 0; f < nf; f++)
+                        GMLE_CK(cudaStreamWaitEvent(m.fork[f], m.ev_fork, 0), "cudaStreamWaitEvent");
+                }
+                for (int l = 0; l < nl; l++) {
+                    const TableLaunch &L = plan.launches[l];
+                    GMLE_CK(cudaGraphLaunch(graphs[slot][L.kind].exec, nl > 1 ? m.fork[l % nf] : s),
+                            "cudaGraphLaunch");
+                    ctx->launches++;
+                }
+                for (int f = 0; nl > 1 && f < nf; f++) {
+                    GMLE_CK(cudaEventRecord(m.ev_join[f], m.fork[f]), "cudaEventRecord");
+                    GMLE_CK(cudaStreamWaitEvent(s, m.ev_join[f], 0), "cudaStreamWaitEvent");
+                }
             }
         }
-        GMLE_CK(cudaEventRecord(step_done[slot], s_step[slot]), "cudaEventRecord");
+        GMLE_CK(cudaEventRecord(step_done[slot], s), "cudaEventRecord");
         return GMLE_OK;
     }
 
@@ -419,7 +441,8 @@ void server_destroy(gmle_ctx *ctx)
     cudaSetDevice(ctx->device);
     for (int k = 0; k < kMaxSlots; k++) {
         if (S->s_step[k]) cudaStreamSynchronize(S->s_step[k]);
-        for (auto &g : S->graphs[k]) cudaGraphExecDestroy(g.second);
+        for (auto &g : S->graphs[k])
+            if (g.exec) cudaGraphExecDestroy(g.exec);
         free_mixed_set(S->sets[k]);
         if (S->s_step[k]) cudaStreamDestroy(S->s_step[k]);
         if (S->step_done[k]) cudaEventDestroy(S->step_done[k]);
