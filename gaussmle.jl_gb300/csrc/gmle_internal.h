@@ -120,6 +120,8 @@ struct gmle_ctx {
     float *d_var = nullptr, *d_gain = nullptr, *d_offset = nullptr;
     int32_t ny = 0, nx = 0;
     unsigned long long *d_bad = nullptr;
+    float *d_pv = nullptr;        // gmle_pvalues: device llr and p-values
+    int64_t pv_cap = 0;
     int64_t launches = 0;
     std::map<std::tuple<int, int, int>, gmle_rt::Tuning> tuning;
     gmle_rt::Slot slots[2];

@@ -301,6 +301,7 @@ void gmle_destroy(gmle_ctx *ctx)
     cudaFree(ctx->d_gain);
     cudaFree(ctx->d_offset);
     cudaFree(ctx->d_bad);
+    cudaFree(ctx->d_pv);
     if (ctx->s_fit) cudaStreamDestroy(ctx->s_fit);
     if (ctx->s_h2d) cudaStreamDestroy(ctx->s_h2d);
     if (ctx->s_d2h) cudaStreamDestroy(ctx->s_d2h);

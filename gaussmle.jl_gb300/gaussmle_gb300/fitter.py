@@ -121,10 +121,13 @@ class LocalizationResult:
         return out
 
 
-def _pvalues(llr: np.ndarray, box: int, nparams: int) -> np.ndarray:
-    """1 - cdf(Chisq(box^2 - P), -2 llr), src/interface.jl:265-275."""
-    from scipy.stats import chi2
-    return (1.0 - chi2.cdf(-2.0 * llr.astype(np.float64), box * box - nparams)).astype(np.float32)
+def _pvalues(ctx: _lib.Context, llr: np.ndarray, box: int, nparams: int) -> np.ndarray:
+    """1 - cdf(Chisq(box^2 - P), -2 llr) (src/interface.jl:265-275), on the GPU."""
+    llr = np.ascontiguousarray(llr, dtype=np.float32)
+    pv = np.empty_like(llr)
+    ctx.check(ctx.lib.gmle_pvalues(ctx.handle, llr.ctypes.data_as(C.c_void_p), llr.size,
+                                   box * box - nparams, pv.ctypes.data_as(C.c_void_p)))
+    return pv
 
 
 def _run(fitter: GaussMLEFitter, data_f: np.ndarray, psf_pixels: PSFModel, camera: int,
@@ -169,7 +172,7 @@ def fit(fitter: GaussMLEFitter, data, variance_map: np.ndarray | None = None):
                                                None, None, vm.shape[0], vm.shape[1]))
         camera = _lib.CAMERA_SCMOS
     params, crlb, llr, flags = _run(fitter, data_f, psf_pixels, camera, xc, yc)
-    pv = _pvalues(llr, box, psf_pixels.nparams)
+    pv = _pvalues(fitter.context, llr, box, psf_pixels.nparams)
     return LocalizationResult(params, crlb, llr, pv, flags,
                               (xc + params[:, 0] - 1).astype(np.float32),
                               (yc + params[:, 1] - 1).astype(np.float32),
@@ -207,7 +210,7 @@ def _fit_batch(fitter: GaussMLEFitter, batch: ROIBatch):
         raise TypeError(f"unsupported camera {type(cam).__name__}")
     params, crlb, llr, flags = _run(fitter, data_f, psf_pixels, camera,
                                     batch.x_corners, batch.y_corners)
-    pv = _pvalues(llr, box, psf_pixels.nparams)
+    pv = _pvalues(fitter.context, llr, box, psf_pixels.nparams)
     return LocalizationResult(params, crlb, llr, pv, flags,
                               (batch.x_corners + params[:, 0] - 1).astype(np.float32),
                               (batch.y_corners + params[:, 1] - 1).astype(np.float32),

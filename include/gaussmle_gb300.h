@@ -173,6 +173,19 @@ gmle_status gmle_autotune(gmle_ctx *ctx, const gmle_fit_desc *desc, const float 
                           float *d_params, float *d_crlb, float *d_llr, uint8_t *d_flags,
                           int32_t *threads_per_roi, int32_t *rois_per_block, float *ms_per_fit);
 
+/*
+ * Goodness-of-fit p-values, computed on the GPU.  Replaces the host loop after
+ * every fit (src/interface.jl:265-275, :459-468): chi2 = -2 llr in Float32 and
+ * p = 1 - Float32(cdf(Chisq(df), chi2)), with df = box^2 - P for a fit of P
+ * parameters.  cdf is evaluated in FP64 (the regularised incomplete gamma
+ * function P(df/2, chi2/2)).  A NaN llr gives a NaN p-value; chi2 <= 0 gives 1.
+ * gmle_pvalues takes host arrays and returns when the p-values are written;
+ * gmle_pvalues_device takes device arrays and enqueues on `stream`.
+ */
+gmle_status gmle_pvalues(gmle_ctx *ctx, const float *llr, int64_t n, int32_t df, float *pvalues);
+gmle_status gmle_pvalues_device(gmle_ctx *ctx, const float *d_llr, int64_t n, int32_t df,
+                                float *d_pvalues, void *stream);
+
 /* Number of fit-kernel launches this context has issued (for accounting). */
 int64_t gmle_kernel_launches(const gmle_ctx *ctx);
 

@@ -122,3 +122,16 @@ def crlb_at(model: int, box: int, psf, theta, precision: str = "f64"):
 
 def max_threads() -> int:
     return int(lib().oracle_max_threads())
+
+
+def pvalues(llr: np.ndarray, df: int) -> np.ndarray:
+    """The reference's goodness-of-fit p-values (src/interface.jl:265-275):
+    chi2 = -2 llr in Float32, p = 1 - Float32(cdf(Chisq(df), chi2)), the cdf
+    in Float64 with chi2 clamped at 0 (Distributions.jl / StatsFuns gammacdf).
+    scipy's regularised incomplete gamma function stands in for
+    SpecialFunctions.gamma_inc."""
+    from scipy.special import gammainc
+    chi2 = (np.float32(-2.0) * np.asarray(llr, np.float32)).astype(np.float64)
+    cdf = gammainc(0.5 * df, 0.5 * np.maximum(chi2, 0.0))
+    cdf = np.where(np.isnan(chi2), np.nan, cdf)
+    return (np.float32(1.0) - cdf.astype(np.float32)).astype(np.float32)

@@ -102,3 +102,18 @@ def test_zero_iterations_returns_the_initial_estimate():
     assert abs(r["params"][0, 3] - edge.mean()) < 1e-3
     sig = np.maximum(0, roi - edge.mean()).sum()
     assert abs(r["params"][0, 2] - max(sig, 100)) / max(sig, 100) < 1e-5
+
+
+def test_oracle_pvalues_known_answers():
+    """The p-value formula of src/interface.jl:265-275 on closed forms and the
+    5% critical values of the chi-square distribution."""
+    x = np.array([0.0, 1.0, 4.0, 10.0])
+    llr = (-0.5 * x).astype(np.float32)
+    # df = 2: cdf(x) = 1 - exp(-x/2), so p = 1 - Float32(1 - exp(-x/2))
+    want = np.float32(1) - (1 - np.exp(-0.5 * x)).astype(np.float32)
+    np.testing.assert_array_equal(O.pvalues(llr, 2), want)
+    for df, crit in ((1, 3.841459), (10, 18.307038)):
+        p = O.pvalues(np.array([-0.5 * crit], np.float32), df)[0]
+        assert abs(p - 0.05) < 2e-6, (df, p)
+    assert np.isnan(O.pvalues(np.array([np.nan], np.float32), 5)[0])
+    assert O.pvalues(np.array([3.0], np.float32), 5)[0] == 1.0  # chi2 < 0 clamps to 0
