@@ -121,4 +121,22 @@ function fit!(results::Matrix{Float32}, uncertainties::Matrix{Float32},
     return flags
 end
 
+"""
+    pvalues(log_likelihoods, box, nparams; ctx)
+
+The p-value loop after the GPU branch (src/interface.jl:265-275), on the GPU:
+`1 - Float32(cdf(Chisq(box^2 - nparams), -2 llr))`.
+"""
+function pvalues(log_likelihoods::Vector{Float32}, box::Integer, nparams::Integer;
+                 ctx::Context = default_context())
+    pv = Vector{Float32}(undef, length(log_likelihoods))
+    GC.@preserve log_likelihoods pv begin
+        st = ccall((:gmle_pvalues, libgmle), Cint,
+                   (Ptr{Cvoid}, Ptr{Float32}, Int64, Int32, Ptr{Float32}),
+                   ctx.ptr, log_likelihoods, length(log_likelihoods), Int32(box^2 - nparams), pv)
+    end
+    check(ctx, st)
+    return pv
+end
+
 end # module
