@@ -313,6 +313,26 @@ def extras(torch, ctx, dev, steps, peak_inst):
                      "roofline_frac": n * w["fp32_equiv"] / per / 1e12 / peak_inst}
         del wl, prm, crl, llr, flg
         torch.cuda.empty_cache()
+    # ROI extraction from device-resident frames (gmle_cut_rois_device): an
+    # HBM-bound copy; 100 frames of 2048 x 2048 (1.7 GB) and 2e6 11x11 ROIs
+    # (0.97 GB out), both larger than L2
+    box, n, nf = 11, 2_000_000, 100
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(5)
+    frames = torch.rand((nf, 2048, 2048), device=dev, generator=gen)
+    ri = lambda hi: torch.randint(1, hi, (n,), device=dev, dtype=torch.int32, generator=gen)
+    fidx, xc, yc = ri(nf + 1), ri(2048 - box + 2), ri(2048 - box + 2)
+    rois = torch.empty(n * box * box, device=dev)
+    dt = time_steps(torch, stream, lambda: G.cut_rois(ctx, frames, fidx, xc, yc, box, out=rois,
+                                                      stream=stream), steps, 3)
+    per = dt / steps
+    peak = measured_peaks().get("hbm_gbs", 6800.0)
+    gbs = n * (2 * box * box * 4 + 12) / per / 1e9
+    out["roi-cut-11x11-2e6-from-100-frames-2048x2048"] = {
+        "rois_per_s": n / per, "ms_per_launch": per * 1e3, "achieved_gbs": gbs,
+        "hbm_frac": gbs / peak, "bytes_per_roi": 2 * box * box * 4 + 12}
+    del frames, rois, fidx, xc, yc
+    torch.cuda.empty_cache()
     return out
 
 

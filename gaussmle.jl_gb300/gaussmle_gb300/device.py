@@ -27,3 +27,27 @@ def fit_device(ctx: _lib.Context, desc: _lib.FitDesc, data, x_corners, y_corners
                                  ptr(y_corners), n, ptr(params), ptr(crlb), ptr(llr),
                                  ptr(flags), C.c_void_p(s.cuda_stream))
     ctx.check(st)
+
+
+def cut_rois(ctx: _lib.Context, frames, frame_idx, x_corners, y_corners, box: int, out=None,
+             stream=None):
+    """Cut box x box ROIs out of device-resident frames (gmle_cut_rois_device).
+
+    `frames` is a CUDA float32 tensor holding the Julia (ny, nx, nframes)
+    column-major stack, i.e. a contiguous torch tensor of shape
+    (nframes, nx, ny); frame indices and corners are 1-based int32 CUDA
+    tensors.  Returns (or fills) the ROI-major stack of n*box*box floats that
+    fit_device takes."""
+    import torch
+    if not (frames.is_cuda and frames.is_contiguous() and frames.dim() == 3):
+        raise ValueError("frames must be a contiguous (nframes, nx, ny) CUDA tensor")
+    nframes, nx, ny = frames.shape
+    n = x_corners.shape[0]
+    if out is None:
+        out = torch.empty(n * box * box, dtype=torch.float32, device=frames.device)
+    s = stream if stream is not None else torch.cuda.current_stream(frames.device)
+    ptr = lambda t: C.c_void_p(t.data_ptr())
+    ctx.check(ctx.lib.gmle_cut_rois_device(ctx.handle, ptr(frames), ny, nx, nframes,
+                                           ptr(frame_idx), ptr(x_corners), ptr(y_corners), n,
+                                           box, ptr(out), C.c_void_p(s.cuda_stream)))
+    return out

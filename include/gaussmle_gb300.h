@@ -174,6 +174,23 @@ gmle_status gmle_autotune(gmle_ctx *ctx, const gmle_fit_desc *desc, const float 
                           int32_t *threads_per_roi, int32_t *rois_per_block, float *ms_per_fit);
 
 /*
+ * Cut n box x box ROIs out of device-resident camera frames into the
+ * (box, box, n) stack that gmle_fit_device takes.  In the reference pipeline a
+ * box finder does this on the host and hands GaussMLE a ROIBatch of ROI stack,
+ * corners and frame indices (examples/full_pipeline_boxer.jl:72-103).
+ * frames: Float32 (ny, nx, nframes) column-major; frame indices and corners:
+ * 1-based Int32, ROI pixel (i, j) of ROI k = frame pixel
+ * (y_corners[k] + i - 1, x_corners[k] + j - 1, frame_idx[k]).  All pointers are
+ * device pointers; the copy is enqueued on `stream`.  An ROI whose frame or box
+ * lies outside the stack is filled with NaN and counted by
+ * gmle_fit_device_errors (synchronise `stream` before asking).
+ */
+gmle_status gmle_cut_rois_device(gmle_ctx *ctx, const float *d_frames, int32_t ny, int32_t nx,
+                                 int64_t nframes, const int32_t *d_frame_idx,
+                                 const int32_t *d_x_corners, const int32_t *d_y_corners,
+                                 int64_t n, int32_t box, float *d_rois, void *stream);
+
+/*
  * Goodness-of-fit p-values, computed on the GPU.  Replaces the host loop after
  * every fit (src/interface.jl:265-275, :459-468): chi2 = -2 llr in Float32 and
  * p = 1 - Float32(cdf(Chisq(df), chi2)), with df = box^2 - P for a fit of P
