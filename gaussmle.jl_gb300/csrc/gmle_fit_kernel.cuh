@@ -937,7 +937,10 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
                 walk_entry<SIG, true>(j + 1, ax, wx, nxp, nxd1, nxd2, nxs1, nxs2);
                 const float npx = N * xp, xp2 = xp * xp;
                 const float *col = pix + (j - 1) * BOX * PS;
-                float A = 0.f, B = 0.f, E = 0.f, F = 0.f, Gc = 0.f;
+                // even and odd rows in separate partial sums: two independent
+                // FMA chains of box/2 instead of one of box
+                float A[2] = {0.f, 0.f}, B[2] = {0.f, 0.f}, E[2] = {0.f, 0.f},
+                      F[2] = {0.f, 0.f}, Gc[2] = {0.f, 0.f};
 #pragma unroll
                 for (int t = 0; t < BOX; t++) {
                     float d, v = 0.f;
@@ -950,15 +953,17 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
                     const float mu = fmaf(npx, py[t], bg);
                     float cf, df;
                     likelihood_terms<SCMOS>(d, v, mu, cf, df);
-                    A = fmaf(py[t], cf, A);
-                    B = fmaf(py2[t], df, B);
-                    E += cf;
-                    F += df;
+                    const int h = t & 1;
+                    A[h] = fmaf(py[t], cf, A[h]);
+                    B[h] = fmaf(py2[t], df, B[h]);
+                    E[h] += cf;
+                    F[h] += df;
                     C[t] = fmaf(xp, cf, C[t]);
                     D[t] = fmaf(xp2, df, D[t]);
-                    if (CROSS) Gc = fmaf(aG[t], df, Gc);
+                    if (CROSS) Gc[h] = fmaf(aG[t], df, Gc[h]);
                 }
-                col_terms<MODEL, P>(gs, hs, xp, xd1, xd2, xs1, xs2, A, B, E, F, Gc, ax, aw);
+                col_terms<MODEL, P>(gs, hs, xp, xd1, xd2, xs1, xs2, A[0] + A[1], B[0] + B[1],
+                                    E[0] + E[1], F[0] + F[1], Gc[0] + Gc[1], ax, aw);
                 xp = nxp; xd1 = nxd1; xd2 = nxd2; xs1 = nxs1; xs2 = nxs2;
             }
 #pragma unroll
@@ -1127,7 +1132,10 @@ __device__ __forceinline__ void fit_rois_tpr(const KernelArgs &a, int64_t roi0, 
                 walk_entry<SIG, true>(j, ax, wx, xp, xd1, xd2, xs1, xs2);
                 const float npx = N * xp, xp2 = xp * xp;
                 const float *col = pix + (j - 1) * BOX * PS;
-                float A = 0.f, B = 0.f, E = 0.f, F = 0.f, Gc = 0.f;
+                // even and odd rows in separate partial sums: two independent
+                // FMA chains of box/2 instead of one of box
+                float A[2] = {0.f, 0.f}, B[2] = {0.f, 0.f}, E[2] = {0.f, 0.f},
+                      F[2] = {0.f, 0.f}, Gc[2] = {0.f, 0.f};
 #pragma unroll
                 for (int t = 0; t < BOX; t++) {
                     float d, v = 0.f;
@@ -1140,15 +1148,17 @@ __device__ __forceinline__ void fit_rois_tpr(const KernelArgs &a, int64_t roi0, 
                     const float mu = fmaf(npx, py[t], bg);
                     float cf, df;
                     likelihood_terms<SCMOS>(d, v, mu, cf, df);
-                    A = fmaf(py[t], cf, A);
-                    B = fmaf(py2[t], df, B);
-                    E += cf;
-                    F += df;
+                    const int h = t & 1;
+                    A[h] = fmaf(py[t], cf, A[h]);
+                    B[h] = fmaf(py2[t], df, B[h]);
+                    E[h] += cf;
+                    F[h] += df;
                     C[t] = fmaf(xp, cf, C[t]);
                     D[t] = fmaf(xp2, df, D[t]);
-                    if (CROSS) Gc = fmaf(aG[t], df, Gc);
+                    if (CROSS) Gc[h] = fmaf(aG[t], df, Gc[h]);
                 }
-                col_terms<MODEL, P>(gs, hs, xp, xd1, xd2, xs1, xs2, A, B, E, F, Gc, ax, aw);
+                col_terms<MODEL, P>(gs, hs, xp, xd1, xd2, xs1, xs2, A[0] + A[1], B[0] + B[1],
+                                    E[0] + E[1], F[0] + F[1], Gc[0] + Gc[1], ax, aw);
             }
 #pragma unroll
             for (int k = 0; k < P; k++) {
