@@ -365,16 +365,25 @@ __device__ void initialize(const float *roi_pix, const float *psf, float *th)
 template <int P>
 __device__ uint8_t crlb_from_fisher(double (&F)[P][P], float *crlb)
 {
-    double m = fabs(F[0][0]);
+    // max |F| (F is symmetric: its upper triangle).  The bit patterns of
+    // non-negative doubles order like their values, and |NaN| orders above
+    // +Inf, so an integer maximum of the magnitudes' bits is Julia's maximum,
+    // NaN-propagating, computed on the integer pipe instead of FP64.
+    long long mb = 0;
 #pragma unroll
     for (int k = 0; k < P; k++)
 #pragma unroll
-        for (int l = 0; l < P; l++) m = jl_maxd(m, fabs(F[k][l]));
-    const double reg = (double)1e-10f * m;
+        for (int l = k; l < P; l++)
+            mb = max(mb, __double_as_longlong(F[k][l]) & 0x7fffffffffffffffLL);
+    const double reg = (double)1e-10f * __longlong_as_double(mb);
 #pragma unroll
     for (int k = 0; k < P; k++) F[k][k] += reg;
 
-    double L[P][P];
+    // FP64 divisions and square roots are long instruction sequences on a pipe
+    // that runs at 1/64 of the FP32 rate: each pivot takes one reciprocal
+    // square root, rL[j] = 1 / L[j][j], and every division by a pivot becomes
+    // a product with it (within an FP64 ulp or two of the divisions).
+    double L[P][P], rL[P];
     bool ok = true;
     // static_cholesky_decomposition!, src/unified_kernel.jl:7-29
 #pragma unroll
@@ -386,9 +395,10 @@ __device__ uint8_t crlb_from_fisher(double (&F)[P][P], float *crlb)
             for (int k = 0; k < j; k++) s -= L[i][k] * L[j][k];
             if (i == j) {
                 if (!(s > 0.0) && !isnan(s)) ok = false;
-                L[i][i] = sqrt(s);
+                rL[j] = rsqrt(s);
+                L[j][j] = s * rL[j];
             } else {
-                L[i][j] = s / L[j][j];
+                L[i][j] = s * rL[j];
             }
         }
     }
@@ -399,13 +409,13 @@ __device__ uint8_t crlb_from_fisher(double (&F)[P][P], float *crlb)
         double Li[P][P];
 #pragma unroll
         for (int j = 0; j < P; j++) {
-            Li[j][j] = 1.0 / L[j][j];
+            Li[j][j] = rL[j];
 #pragma unroll
             for (int i = j + 1; i < P; i++) {
                 double s = 0.0;
 #pragma unroll
                 for (int k = j; k < i; k++) s += L[i][k] * Li[k][j];
-                Li[i][j] = -s / L[i][i];
+                Li[i][j] = -s * rL[i];
             }
         }
 #pragma unroll
@@ -464,11 +474,12 @@ __device__ uint8_t crlb_from_fisher(double (&F)[P][P], float *crlb)
             flags = FLAG_SINGULAR;
         }
     }
+    // CRLB = sqrt(max(0, diag)): the output is Float32, so the root is taken
+    // in FP32 of the rounded variance (within an FP32 ulp of the FP64 root)
 #pragma unroll
-    for (int k = 0; k < P; k++) {
-        const double v = (flags == FLAG_SINGULAR) ? diag[k] : sqrt(jl_maxd(0.0, diag[k]));
-        crlb[k] = (float)v;
-    }
+    for (int k = 0; k < P; k++)
+        crlb[k] = (flags == FLAG_SINGULAR) ? (float)diag[k]
+                                           : sqrtf((float)jl_maxd(0.0, diag[k]));
     if (isfinite(crlb[0])) flags |= FLAG_CONVERGED;
     return flags;
 }
