@@ -398,13 +398,14 @@ def run_ours(args):
 
     # ---- each group's launch alone: the dominant kernel and its roofline ----
     per_group = []
-    torch.cuda.nvtx.range_push("per_group")
     for g, b in zip(groups, dgs):
         fn = (lambda g=g, b=b: G.fit_device(ctx, b["group"].desc, g["data"], g["xc"], g["yc"],
                                              b["params"], b["crlb"], b["llr"], b["flags"],
                                              stream=stream))
+        # one range per group (e.g. "group_AstigmaticXYZNB_15"), for profiler filters
+        torch.cuda.nvtx.range_push(f"group_{g['psf'].__class__.__name__}_{g['box']}")
         per_group.append(time_steps(torch, stream, fn, args.steps, 3) / args.steps)
-    torch.cuda.nvtx.range_pop()
+        torch.cuda.nvtx.range_pop()
     dt_plain_dev = sum(per_group) * args.steps
 
     # ---- the same batch as requests of <= 50000 ROIs: table launches only ----

@@ -641,14 +641,29 @@ __device__ __forceinline__ void stage_block(const KernelArgs &a, float *spix, in
         }
         cp_async_wait_all();
         if (a.adu) {
-#pragma unroll 4
-            for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
-                const int g = e / B2;
-                if (sok[g]) {
-                    const int p = e - g * B2, j = p / BOX, i = p - j * BOX;
-                    const long long m = sbase[g] + i + (long long)a.ny * j;
-                    const float off = __ldg(a.offset + m), gn = __ldg(a.gain + m);
-                    spix[2 * e] = __fmul_rn(__fadd_rn(spix[2 * e], -off), gn);
+            // The gain and offset gathers (L2-resident maps) of kU pixels are
+            // issued before any is used, so that they overlap.
+            constexpr int kU = 16;
+            for (int e0 = threadIdx.x; e0 < cnt; e0 += kU * blockDim.x) {
+                float off[kU], gn[kU];
+#pragma unroll
+                for (int u = 0; u < kU; u++) {
+                    const int e = e0 + u * blockDim.x;
+                    off[u] = 0.f;
+                    gn[u] = 1.f;
+                    const int g = e / B2;
+                    if (e < cnt && sok[g]) {
+                        const int p = e - g * B2, j = p / BOX, i = p - j * BOX;
+                        const long long m = sbase[g] + i + (long long)a.ny * j;
+                        off[u] = __ldg(a.offset + m);
+                        gn[u] = __ldg(a.gain + m);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < kU; u++) {
+                    const int e = e0 + u * blockDim.x;
+                    if (e < cnt && sok[e / B2])
+                        spix[2 * e] = __fmul_rn(__fadd_rn(spix[2 * e], -off[u]), gn[u]);
                 }
             }
         }
