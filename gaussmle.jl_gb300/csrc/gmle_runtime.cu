@@ -758,26 +758,29 @@ gmle_status enqueue_table_launch(gmle_ctx *ctx, MixedSet &m, const TableLaunch &
 
 gmle_status enqueue_plan(gmle_ctx *ctx, MixedSet &m, const MixedPlan &plan, cudaStream_t s)
 {
-    // Table launches of different kinds run concurrently with each other and
-    // with the plain launches (on the fork streams, joined back into s): each
-    // persistent grid's tail overlaps the next launch.
-    const int nl = (int)plan.launches.size();
-    const bool fork = nl > 1 || (nl == 1 && !plan.plain.empty());
-    const int nf = fork ? std::min(nl, kForks) : 0;
+    // All launches of a plan (plain launches of large groups, table launches
+    // of the rest) run concurrently on the fork streams, joined back into s:
+    // each launch's last, partly filled wave overlaps the others.
+    const int np = (int)plan.plain.size(), nl = (int)plan.launches.size();
+    const int units = np + nl;
+    const bool fork = units > 1;
+    const int nf = fork ? std::min(units, kForks) : 0;
     if (fork) {
         CK(cudaEventRecord(m.ev_fork, s), "cudaEventRecord");
         for (int f = 0; f < nf; f++)
             CK(cudaStreamWaitEvent(m.fork[f], m.ev_fork, 0), "cudaStreamWaitEvent");
     }
-    for (const gmle_group &G : plan.plain) {
+    for (int u = 0; u < np; u++) {
+        const gmle_group &G = plan.plain[u];
         const Tuning t = pick_tuning(ctx, &G.desc, G.n);
         KernelArgs a = make_args(ctx, &G.desc, G.data, G.x_corners, G.y_corners, G.n, G.params,
                                  G.crlb, G.llr, G.flags, t.tpr);
-        CK(launch(ctx, &G.desc, a, t.rois_per_block, s), "fit kernel launch");
+        CK(launch(ctx, &G.desc, a, t.rois_per_block, fork ? m.fork[u % nf] : s),
+           "fit kernel launch");
     }
     for (int l = 0; l < nl; l++) {
         const gmle_status st = enqueue_table_launch(ctx, m, plan.launches[l],
-                                                    fork ? m.fork[l % nf] : s);
+                                                    fork ? m.fork[(np + l) % nf] : s);
         if (st != GMLE_OK) return st;
     }
     for (int f = 0; f < nf; f++) {
