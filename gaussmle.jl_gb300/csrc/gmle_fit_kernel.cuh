@@ -491,10 +491,15 @@ __device__ uint8_t crlb_from_fisher(double (&F)[P][P], float *crlb)
 // float2 (data in e-, read-noise variance) for sCMOS), for sCMOS the map
 // offset of each ROI's first pixel (int64), one ok flag per slot, and, when
 // several lanes share a ROI (tpr > 1), NT * BOX y-axis table entries.
+//
+// One thread per ROI (tpr == 1) with sCMOS data keeps only the data plane in
+// shared memory: each thread's variance tile lives in its tensor-memory lane
+// (TmemVar below), which halves the shared memory per resident ROI.
 __host__ __device__ inline size_t smem_bytes(int model, int box, bool scmos, int tpr, int rois)
 {
     const int nt = model == 0 ? 3 : 5;
-    return (size_t)rois * (sizeof(float) * ((size_t)box * box * (scmos ? 2 : 1) +
+    const bool var_in_smem = scmos && tpr > 1;
+    return (size_t)rois * (sizeof(float) * ((size_t)box * box * (var_in_smem ? 2 : 1) +
                                             (tpr > 1 ? (size_t)nt * box : 0)) +
                            (scmos ? sizeof(long long) : 0) + sizeof(int));
 }
@@ -590,17 +595,167 @@ __device__ __forceinline__ void cp_async_wait_all()
     asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
 }
 
+// ---- tensor memory (TMEM) as per-thread storage ------------------------------
+//
+// Blackwell's tensor memory (128 lanes x 512 32-bit columns per SM) is
+// otherwise idle in this kernel.  The one-thread-per-ROI sCMOS kernel keeps
+// each ROI's variance tile there: thread i of warp w owns TMEM lane
+// 32 (w % 4) + i (a warp reaches only its lane quarter), pixel p of its ROI is
+// column p of the CTA's allocation, and each fitted column is read back with
+// one tcgen05.ld.  Allocation is by columns across all 128 lanes, so CTAs of
+// four warps use it fully.  Warp 0 allocates at kernel start and frees it at
+// kernel end, on every path; a CTA that finds TMEM full waits in
+// tcgen05.alloc until a resident CTA frees its columns.
+template <int BOX> struct TmemVar {
+    static constexpr int B2 = BOX * BOX;
+    static constexpr int LW = BOX <= 8 ? 8 : 16;  // columns of one per-column load
+    static constexpr int CHUNKS = (B2 + 15) / 16;  // 16-column stores of a tile
+    static constexpr int NEED = CHUNKS * 16 > BOX * (BOX - 1) + LW ? CHUNKS * 16
+                                                                   : BOX * (BOX - 1) + LW;
+    static constexpr int NCOLS = NEED <= 32 ? 32 : NEED <= 64 ? 64 : NEED <= 128 ? 128
+                               : NEED <= 256 ? 256 : 512;
+    static_assert(NEED <= 512, "variance tile larger than tensor memory");
+};
+
+__host__ __device__ constexpr int tmem_var_cols(int box)
+{
+    return box == 5 ? TmemVar<5>::NCOLS : box == 7 ? TmemVar<7>::NCOLS
+         : box == 9 ? TmemVar<9>::NCOLS : box == 11 ? TmemVar<11>::NCOLS
+         : box == 13 ? TmemVar<13>::NCOLS : TmemVar<15>::NCOLS;
+}
+
+template <int NCOLS>
+__device__ __forceinline__ void tmem_alloc(uint32_t *s_dst)  // one full warp
+{
+    const uint32_t dst = (uint32_t)__cvta_generic_to_shared(s_dst);
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 :: "r"(dst), "n"(NCOLS) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+template <int NCOLS>
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr)  // one full warp
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
+                 :: "r"(taddr), "n"(NCOLS) : "memory");
+}
+// Around a CTA barrier that orders tensor-memory accesses.
+__device__ __forceinline__ void tmem_sync()
+{
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16])
+{
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, "
+                 "%8, %9, %10, %11, %12, %13, %14, %15, %16};"
+                 :: "r"(taddr), "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]),
+                    "f"(v[6]), "f"(v[7]), "f"(v[8]), "f"(v[9]), "f"(v[10]), "f"(v[11]),
+                    "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15])
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st()
+{
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+// Load LW (8 or 16) consecutive columns of this thread's lane; waits for them.
+template <int LW>
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, float (&v)[LW])
+{
+    if constexpr (LW == 16) {
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, "
+                     "%8, %9, %10, %11, %12, %13, %14, %15}, [%16];\n"
+                     "tcgen05.wait::ld.sync.aligned;"
+                     : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]),
+                       "=f"(v[6]), "=f"(v[7]), "=f"(v[8]), "=f"(v[9]), "=f"(v[10]), "=f"(v[11]),
+                       "=f"(v[12]), "=f"(v[13]), "=f"(v[14]), "=f"(v[15])
+                     : "r"(taddr) : "memory");
+    } else {
+        static_assert(LW == 8, "8 or 16 columns");
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, "
+                     "[%8];\n"
+                     "tcgen05.wait::ld.sync.aligned;"
+                     : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]),
+                       "=f"(v[6]), "=f"(v[7])
+                     : "r"(taddr) : "memory");
+    }
+}
+
+// ADU -> e- of the staged pixels (PS floats apart), (ADU - offset) * gain
+// (src/camera_models.jl:110-113).  The gain and offset gathers (L2-resident
+// maps) of kU pixels are issued before any is used, so that they overlap.
+template <int BOX, int PS>
+__device__ __forceinline__ void adu_to_electrons(const KernelArgs &a, float *spix, const int *sok,
+                                                 const long long *sbase, int cnt)
+{
+    constexpr int B2 = BOX * BOX;
+    constexpr int kU = 16;
+    for (int e0 = threadIdx.x; e0 < cnt; e0 += kU * blockDim.x) {
+        float off[kU], gn[kU];
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            const int e = e0 + u * blockDim.x;
+            off[u] = 0.f;
+            gn[u] = 1.f;
+            const int g = e / B2;
+            if (e < cnt && sok[g]) {
+                const int p = e - g * B2, j = p / BOX, i = p - j * BOX;
+                const long long m = sbase[g] + i + (long long)a.ny * j;
+                off[u] = __ldg(a.offset + m);
+                gn[u] = __ldg(a.gain + m);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            const int e = e0 + u * blockDim.x;
+            if (e < cnt && sok[e / B2])
+                spix[PS * e] = __fmul_rn(__fadd_rn(spix[PS * e], -off[u]), gn[u]);
+        }
+    }
+}
+
+// Variance tile of this thread's ROI (slot threadIdx.x) into its TMEM lane,
+// pixel p at column p; zeros for an empty or rejected slot.  Every thread of
+// the block calls it (the stores are warp-wide).
+template <int BOX>
+__device__ __forceinline__ void stage_var_tmem(const KernelArgs &a, const float *spix,
+                                               const int *sok, int R, int nroi, uint32_t taddr)
+{
+    constexpr int B2 = BOX * BOX;
+    const long long *sbase = reinterpret_cast<const long long *>(spix + R * B2);
+    const int g = threadIdx.x;
+    const bool ok = g < nroi && sok[g];
+    const long long base = ok ? sbase[g] : 0;
+#pragma unroll
+    for (int c = 0; c < TmemVar<BOX>::CHUNKS; c++) {
+        float v[16];
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+            const int p = 16 * c + u;
+            const int j = p / BOX, i = p - j * BOX;
+            v[u] = (ok && p < B2) ? __ldg(a.var + base + i + (long long)a.ny * j) : 0.f;
+        }
+        tmem_st16(taddr + 16 * c, v);
+    }
+    tmem_wait_st();
+}
+
 // Stage the block's R ROIs (contiguous in global memory) into shared memory.
 // All pixel (and variance-tile) copies of a thread are issued as cp.async
 // before any is waited for; for sCMOS the variance tile is gathered from the
 // resident map and ADU data are converted, (ADU - offset) * gain
 // (src/camera_models.jl:110-113), with the gain/offset loads batched.
-template <int BOX, bool SCMOS>
+//
+// With TM (sCMOS, one thread per ROI) only the data plane is staged here, with
+// the Poisson path's contiguous copies; the variance tiles go to tensor memory
+// (stage_var_tmem).
+template <int BOX, bool SCMOS, bool TM = false>
 __device__ __forceinline__ void stage_block(const KernelArgs &a, float *spix, int *sok, int R,
                                             int64_t roi0, int nroi)
 {
     constexpr int B2 = BOX * BOX;
-    long long *sbase = reinterpret_cast<long long *>(spix + R * B2 * (SCMOS ? 2 : 1));
+    constexpr int PS = (SCMOS && !TM) ? 2 : 1;  // floats per staged pixel
+    long long *sbase = reinterpret_cast<long long *>(spix + R * B2 * PS);
     for (int g = threadIdx.x; g < R; g += blockDim.x) {
         int ok = g < nroi;
         long long base = 0;
@@ -615,7 +770,7 @@ __device__ __forceinline__ void stage_block(const KernelArgs &a, float *spix, in
     }
     const float *src = a.data + roi0 * B2;
     const int cnt = nroi * B2;
-    if (!SCMOS) {
+    if (!SCMOS || TM) {
         if ((reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
             const int c4 = cnt >> 2;
             for (int e = threadIdx.x; e < c4; e += blockDim.x)
@@ -627,6 +782,10 @@ __device__ __forceinline__ void stage_block(const KernelArgs &a, float *spix, in
         }
         for (int e = cnt + threadIdx.x; e < R * B2; e += blockDim.x) spix[e] = 0.f;
         cp_async_wait_all();
+        if (SCMOS && a.adu) {
+            __syncthreads();  // the copies of other threads, sok and sbase
+            adu_to_electrons<BOX, 1>(a, spix, sok, sbase, cnt);
+        }
     } else {
         __syncthreads();  // sok, sbase
         // consecutive e walk down a column: contiguous map addresses
@@ -640,33 +799,7 @@ __device__ __forceinline__ void stage_block(const KernelArgs &a, float *spix, in
             cp_async4(spix + 2 * e + 1, okg ? a.var + m : a.var, okg ? 4u : 0u);
         }
         cp_async_wait_all();
-        if (a.adu) {
-            // The gain and offset gathers (L2-resident maps) of kU pixels are
-            // issued before any is used, so that they overlap.
-            constexpr int kU = 16;
-            for (int e0 = threadIdx.x; e0 < cnt; e0 += kU * blockDim.x) {
-                float off[kU], gn[kU];
-#pragma unroll
-                for (int u = 0; u < kU; u++) {
-                    const int e = e0 + u * blockDim.x;
-                    off[u] = 0.f;
-                    gn[u] = 1.f;
-                    const int g = e / B2;
-                    if (e < cnt && sok[g]) {
-                        const int p = e - g * B2, j = p / BOX, i = p - j * BOX;
-                        const long long m = sbase[g] + i + (long long)a.ny * j;
-                        off[u] = __ldg(a.offset + m);
-                        gn[u] = __ldg(a.gain + m);
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < kU; u++) {
-                    const int e = e0 + u * blockDim.x;
-                    if (e < cnt && sok[e / B2])
-                        spix[2 * e] = __fmul_rn(__fadd_rn(spix[2 * e], -off[u]), gn[u]);
-                }
-            }
-        }
+        if (a.adu) adu_to_electrons<BOX, 2>(a, spix, sok, sbase, cnt);
     }
     __syncthreads();
 }
@@ -898,20 +1031,22 @@ __device__ __forceinline__ void axis_widths(const float *th, const KernelArgs &a
 // per block, the persistent mixed-batch kernel once per work tile.
 template <int MODEL, int BOX, bool SCMOS>
 __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, int nroi,
-                                            float *smem)
+                                            float *smem, uint32_t taddr)
 {
     constexpr int P = ModelInfo<MODEL>::P;
     constexpr bool SIG = ModelInfo<MODEL>::SIG;
     constexpr bool CROSS = (MODEL == 1 || MODEL == 3);
     constexpr int B2 = BOX * BOX;
-    constexpr int PS = SCMOS ? 2 : 1;
+    constexpr int PS = 1;  // data plane; sCMOS variance tiles are in tensor memory
     constexpr int NB = SIG ? 4 : 3;
+    constexpr int LW = TmemVar<BOX>::LW;
     using S = Slots<MODEL>;
 
     const int R = blockDim.x;
     float *spix = smem;
-    int *sok = reinterpret_cast<int *>(spix + R * B2 * PS + (SCMOS ? 2 * R : 0));
-    stage_block<BOX, SCMOS>(a, spix, sok, R, roi0, nroi);
+    int *sok = reinterpret_cast<int *>(spix + R * B2 + (SCMOS ? 2 * R : 0));
+    stage_block<BOX, SCMOS, true>(a, spix, sok, R, roi0, nroi);
+    if (SCMOS) stage_var_tmem<BOX>(a, spix, sok, R, nroi, taddr);
 
     const int g = threadIdx.x;
     if (__all_sync(0xffffffffu, g >= nroi)) return;
@@ -963,19 +1098,16 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
                 walk_entry<SIG, true>(j + 1, ax, wx, nxp, nxd1, nxd2, nxs1, nxs2);
                 const float npx = N * xp, xp2 = xp * xp;
                 const float *col = pix + (j - 1) * BOX * PS;
+                float vv[LW];  // this column's variances, from tensor memory
+                if (SCMOS) tmem_ld<LW>(taddr + BOX * (j - 1), vv);
                 // even and odd rows in separate partial sums: two independent
                 // FMA chains of box/2 instead of one of box
                 float A[2] = {0.f, 0.f}, B[2] = {0.f, 0.f}, E[2] = {0.f, 0.f},
                       F[2] = {0.f, 0.f}, Gc[2] = {0.f, 0.f};
 #pragma unroll
                 for (int t = 0; t < BOX; t++) {
-                    float d, v = 0.f;
-                    if (SCMOS) {
-                        const float2 q = reinterpret_cast<const float2 *>(col)[t];
-                        d = q.x; v = q.y;
-                    } else {
-                        d = col[t];
-                    }
+                    const float d = col[t];
+                    const float v = SCMOS ? vv[t] : 0.f;
                     const float mu = fmaf(npx, py[t], bg);
                     float cf, df;
                     likelihood_terms<SCMOS>(d, v, mu, cf, df);
@@ -1009,6 +1141,8 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
                 walk_entry<SIG, false>(j + 1, ax, wx, nxp, nxd1, nxd2, nxs1, nxs2);
                 const float npx = N * xp;
                 const float *col = pix + (j - 1) * BOX * PS;
+                float vv[LW];  // this column's variances, from tensor memory
+                if (SCMOS) tmem_ld<LW>(taddr + BOX * (j - 1), vv);
                 float Q[NB][NB];
 #pragma unroll
                 for (int p = 0; p < NB; p++)
@@ -1016,13 +1150,8 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
                     for (int q = 0; q < NB; q++) Q[p][q] = 0.f;
 #pragma unroll
                 for (int t = 0; t < BOX; t++) {
-                    float d, v = 0.f;
-                    if (SCMOS) {
-                        const float2 q = reinterpret_cast<const float2 *>(col)[t];
-                        d = q.x; v = q.y;
-                    } else {
-                        d = col[t];
-                    }
+                    const float d = col[t];
+                    const float v = SCMOS ? vv[t] : 0.f;
                     const float mu = fmaf(npx, py[t], bg);
                     final_pixel<SCMOS, SIG, NB>(d, v, mu, py[t], yd1[t], SIG ? ys1[t] : 0.f, llr, Q);
                 }
@@ -1047,24 +1176,40 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
 // (`a` supplies only tpr); the block fits tiles of the table's groups, each
 // through the block's shared-memory copy of the tile's group arguments, until
 // none is left.
+//
+// sCMOS: warp 0 allocates the CTA's tensor memory for the variance tiles before
+// the first tile and frees it after the last; no path leaves the kernel
+// between the two.
 template <int MODEL, int BOX, bool SCMOS, bool TABLE>
-__global__ void __launch_bounds__(64) fit_kernel_r1(const KernelArgs a, const TileTable t)
+__global__ void __launch_bounds__(128) fit_kernel_r1(const KernelArgs a, const TileTable t)
 {
     extern __shared__ __align__(16) float smem[];
+    __shared__ uint32_t s_tmem;
+    constexpr int NCOLS = TmemVar<BOX>::NCOLS;
     const int R = blockDim.x;
+    uint32_t taddr = 0;
+    if (SCMOS) {
+        if (threadIdx.x < 32) tmem_alloc<NCOLS>(&s_tmem);
+        tmem_sync();
+        taddr = s_tmem + ((uint32_t)(((threadIdx.x >> 5) & 3) * 32) << 16);
+    }
     if (!TABLE) {
         const int64_t roi0 = (int64_t)blockIdx.x * R;
         const int64_t left = a.n - roi0;
-        fit_rois_r1<MODEL, BOX, SCMOS>(a, roi0, left < R ? (int)left : R, smem);
-        return;
+        fit_rois_r1<MODEL, BOX, SCMOS>(a, roi0, left < R ? (int)left : R, smem, taddr);
+    } else {
+        TableSlot *ts = table_slot(smem, smem_bytes(MODEL, BOX, SCMOS, 1, R));
+        table_slot_init(ts);
+        int64_t roi0;
+        int nroi;
+        while (table_next(t, R, ts, roi0, nroi)) {
+            fit_rois_r1<MODEL, BOX, SCMOS>(ts->a, roi0, nroi, smem, taddr);
+            __syncthreads();  // the tile's shared memory and slot are free again
+        }
     }
-    TableSlot *ts = table_slot(smem, smem_bytes(MODEL, BOX, SCMOS, 1, R));
-    table_slot_init(ts);
-    int64_t roi0;
-    int nroi;
-    while (table_next(t, R, ts, roi0, nroi)) {
-        fit_rois_r1<MODEL, BOX, SCMOS>(ts->a, roi0, nroi, smem);
-        __syncthreads();  // the tile's shared memory and slot are free again
+    if (SCMOS) {
+        tmem_sync();  // every warp's tensor-memory loads have completed
+        if (threadIdx.x < 32) tmem_dealloc<NCOLS>(s_tmem);
     }
 }
 

@@ -4,6 +4,8 @@
 // the eight units compile in parallel.
 #pragma once
 
+#include <algorithm>
+
 #include "gmle_fit_kernel.cuh"
 
 namespace gmle {
@@ -21,7 +23,7 @@ __host__ __device__ constexpr int box_index(int box)
 inline bool box_supported(int box) { return box_index(box) >= 0; }
 
 // Largest block of the one-thread-per-ROI kernel (its __launch_bounds__).
-constexpr int kMaxThreadsR1 = 64;
+constexpr int kMaxThreadsR1 = 128;
 
 // One launch of a model's kernel.  Plain (t.header == nullptr): ceil(a.n / rpb)
 // blocks over `a`.  Table: `grid` persistent blocks over the table's groups,
@@ -56,8 +58,9 @@ inline cudaError_t launch_fit(int model, int box, bool scmos, const KernelArgs &
 #undef GMLE_CASE
 }
 
-// Resident blocks per SM of a table launch of this shape (0 on error); also
-// sets the kernel's shared-memory limit on the current device.
+// Resident blocks per SM of a table launch of this shape (0 if none fits; a
+// negated cudaError_t on error); also sets the kernel's shared-memory limit on
+// the current device.
 inline int table_blocks_per_sm(int model, int box, bool scmos, int tpr, int rois_per_block)
 {
 #define GMLE_CASE(M)                                                        \
@@ -86,8 +89,8 @@ cudaError_t kernel_for(int tpr, bool table, FitKernel *kern)
     const bool r1 = tpr == 1;
     *kern = r1 ? (table ? fit_kernel_r1<MODEL, BOX, SCMOS, true> : fit_kernel_r1<MODEL, BOX, SCMOS, false>)
                : (table ? fit_kernel<MODEL, BOX, SCMOS, true> : fit_kernel<MODEL, BOX, SCMOS, false>);
-    // The largest dynamic shared memory any shape asks for, once per kernel
-    // and device (setting it twice is harmless).
+    // The largest dynamic shared memory a block may have, once per kernel and
+    // device (setting it twice is harmless).
     constexpr int kMaxDevices = 64;
     static bool done[2][2][kMaxDevices] = {};
     int dev = 0;
@@ -95,7 +98,12 @@ cudaError_t kernel_for(int tpr, bool table, FitKernel *kern)
     if (e != cudaSuccess) return e;
     const bool known = dev >= 0 && dev < kMaxDevices;
     if (known && done[r1][table][dev]) return cudaSuccess;
-    e = cudaFuncSetAttribute(*kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    // the 227 KiB a block may use include the kernel's static shared memory
+    cudaFuncAttributes fa;
+    e = cudaFuncGetAttributes(&fa, *kern);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(*kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             227 * 1024 - (int)fa.sharedSizeBytes);
     if (e == cudaSuccess && known) done[r1][table][dev] = true;
     return e;
 }
@@ -124,11 +132,14 @@ template <int MODEL, int BOX, bool SCMOS>
 int table_blocks_one(int tpr, int rpb)
 {
     FitKernel kern;
-    if (kernel_for<MODEL, BOX, SCMOS>(tpr, true, &kern) != cudaSuccess) return 0;
+    cudaError_t e = kernel_for<MODEL, BOX, SCMOS>(tpr, true, &kern);
+    if (e != cudaSuccess) return -(int)e;
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &nb, kern, rpb * tpr, launch_smem(MODEL, BOX, SCMOS, tpr, rpb, true)) != cudaSuccess)
-        return 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &nb, kern, rpb * tpr, launch_smem(MODEL, BOX, SCMOS, tpr, rpb, true));
+    if (e != cudaSuccess) return -(int)e;
+    // the one-thread sCMOS kernel also holds tensor memory: 512 columns per SM
+    if (SCMOS && tpr == 1) nb = std::min(nb, 512 / tmem_var_cols(BOX));
     return nb;
 }
 

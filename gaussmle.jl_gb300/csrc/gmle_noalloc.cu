@@ -233,8 +233,9 @@ extern "C" gmle_status gmle_fit_mixed_device_noalloc(const gmle_group *groups, i
         const int bps = gmle::table_blocks_per_sm(d0.model, d0.box, scmos, t.tpr, t.rois_per_block);
         if (bps <= 0)
             return report(err, err_len, GMLE_CUDA_ERROR,
-                          "no resident block for model %d box %d (tpr %d, %d ROIs)", d0.model,
-                          d0.box, t.tpr, t.rois_per_block);
+                          "no resident block for model %d box %d (tpr %d, %d ROIs)%s%s", d0.model,
+                          d0.box, t.tpr, t.rois_per_block, bps < 0 ? ": " : "",
+                          bps < 0 ? cudaGetErrorString((cudaError_t)-bps) : "");
         shape[kind] = gmle::LaunchShape{t.tpr, t.rois_per_block,
                                         std::min<int64_t>((int64_t)S.num_sms * bps, tiles)};
         used += cnt;

@@ -90,7 +90,9 @@ Tuning default_tuning(int num_sms, int model, int box, bool scmos, int64_t n)
     while (tpr < 4 && (rois_per_sm * tpr < want_threads_sm ||
                        n * tpr < (int64_t)num_sms * want_threads_sm))
         tpr *= 2;
-    int rpb = tpr == 1 ? 32 : 128 / tpr;
+    // one thread per ROI with sCMOS data: blocks of 4 warps use the tensor
+    // memory that holds the variance tiles fully
+    int rpb = tpr == 1 ? (scmos ? 128 : 32) : 128 / tpr;
     while (rpb * tpr > 32 && gmle::smem_bytes(model, box, scmos, tpr, rpb) > 100 * 1024) rpb /= 2;
     if (rpb * tpr < 32) rpb = 32 / tpr;
     return {tpr, rpb};
@@ -708,8 +710,9 @@ gmle_status plan_mixed(gmle_ctx *ctx, const gmle_group *groups, int32_t ngroups,
         hdr[1] = tiles;
         const int bps = gmle::table_blocks_per_sm(L.model, L.box, L.scmos, t.tpr, rpb);
         if (bps <= 0)
-            return fail(ctx, GMLE_CUDA_ERROR, "no resident block for model %d box %d (tpr %d, %d ROIs)",
-                        L.model, L.box, t.tpr, rpb);
+            return fail(ctx, GMLE_CUDA_ERROR, "no resident block for model %d box %d (tpr %d, %d ROIs)%s%s",
+                        L.model, L.box, t.tpr, rpb, bps < 0 ? ": " : "",
+                        bps < 0 ? cudaGetErrorString((cudaError_t)-bps) : "");
         const int64_t full = (int64_t)ctx->num_sms * bps;
         L.shape = gmle::LaunchShape{t.tpr, rpb, opt.full_grid ? full : std::min(full, tiles)};
         L.groups = hdr[0];
