@@ -55,8 +55,11 @@ WORKLOAD = ("mixed-batch: 40% XYNB 11x11, 25% XYNBS 9x9, 15% XYNBSXSY 13x13, "
 TRAFFIC_BYTES_PER_ROI: dict[str, float] = {
     # 90 000 ROIs, 4 threads per ROI, 32 ROIs/block: 150.3 MB read + 5.8 MB written
     "fit_kernel<3, 15, true, false>": 1734.7,
-    # 240 000 ROIs, one thread per ROI, 32 ROIs/block: 200.7 MB read + 10.3 MB written
-    "fit_kernel_r1<0, 11, true, false>": 879.2,
+    # 90 000 ROIs, one thread per ROI, 128 ROIs/block (variances in tensor
+    # memory): 148.9 MB read + 5.6 MB written
+    "fit_kernel_r1<3, 15, true, false>": 1716.6,
+    # 240 000 ROIs, one thread per ROI, 64 ROIs/block: 201.7 MB read + 10.5 MB written
+    "fit_kernel_r1<0, 11, true, false>": 884.3,
 }
 
 

@@ -156,6 +156,11 @@ gmle_status plan_mixed(gmle_ctx *ctx, const gmle_group *groups, int32_t ngroups,
 // record_reuse each table's reuse event is recorded after its copy.
 gmle_status upload_plan(gmle_ctx *ctx, MixedSet &m, const MixedPlan &plan, cudaStream_t s,
                         bool record_reuse);
+// Whether a launch's kernel keeps tensor memory for its whole duration (the
+// one-thread-per-ROI sCMOS kernel, which holds its variance tiles there).
+inline bool holds_tmem(bool scmos, int tpr) { return scmos && tpr == 1; }
+// Fork stream of a plan's index-th launch among nf forks.
+int plan_stream(int index, bool holds_tmem, int nf);
 // One table launch of a plan on q: its tile counter reset, then the kernel.
 gmle_status enqueue_table_launch(gmle_ctx *ctx, MixedSet &m, const TableLaunch &L, cudaStream_t q);
 // The plan's plain launches on s, then its table launches, concurrently on

@@ -128,19 +128,52 @@ cudaError_t launch_one(const KernelArgs &a, const TileTable &t, const LaunchShap
     return cudaGetLastError();
 }
 
+// Resident blocks per SM of a kernel that holds `cols` tensor-memory columns
+// per block (a negated cudaError_t on error).
+inline int tmem_kernel_blocks_per_sm(FitKernel kern, int threads, size_t dyn_smem, int cols)
+{
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, kern);
+    if (e != cudaSuccess) return -(int)e;
+    int dev = 0, regs_sm = 0, smem_sm = 0, smem_rsv = 0, thr_sm = 0, blk_sm = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&smem_rsv, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&blk_sm, cudaDevAttrMaxBlocksPerMultiprocessor, dev);
+    if (e != cudaSuccess) return -(int)e;
+    const int warps = (threads + 31) / 32;
+    const int regs_warp = ((fa.numRegs + 7) / 8) * 8 * 32;  // allocated per warp in 8-register units
+    const int by_regs = regs_warp > 0 ? (regs_sm / regs_warp) / warps : blk_sm;
+    const size_t per_block = dyn_smem + fa.sharedSizeBytes + (size_t)smem_rsv;
+    const int by_smem = (int)((size_t)smem_sm / per_block);
+    const int by_threads = thr_sm / (warps * 32);
+    const int by_tmem = 512 / cols;
+    return std::max(0, std::min({by_regs, by_smem, by_threads, blk_sm, by_tmem}));
+}
+
 template <int MODEL, int BOX, bool SCMOS>
 int table_blocks_one(int tpr, int rpb)
 {
     FitKernel kern;
     cudaError_t e = kernel_for<MODEL, BOX, SCMOS>(tpr, true, &kern);
     if (e != cudaSuccess) return -(int)e;
+    const size_t smem = launch_smem(MODEL, BOX, SCMOS, tpr, rpb, true);
     int nb = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &nb, kern, rpb * tpr, launch_smem(MODEL, BOX, SCMOS, tpr, rpb, true));
-    if (e != cudaSuccess) return -(int)e;
-    // the one-thread sCMOS kernel also holds tensor memory: 512 columns per SM
-    if (SCMOS && tpr == 1) nb = std::min(nb, 512 / tmem_var_cols(BOX));
-    return nb;
+    if (!(SCMOS && tpr == 1)) {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, rpb * tpr, smem);
+        return e == cudaSuccess ? nb : -(int)e;
+    }
+    // The one-thread sCMOS kernel allocates tensor memory, for which the
+    // occupancy API answers one block per SM (it cannot know how many columns
+    // a block takes).  Its residency is computed here from its registers,
+    // shared memory and threads, and the 512 columns an SM holds.
+    return tmem_kernel_blocks_per_sm(kern, rpb * tpr, smem, tmem_var_cols(BOX));
 }
 
 #define GMLE_BOX_SWITCH(CALL)       \

@@ -536,8 +536,14 @@ gmle_status gmle_autotune(gmle_ctx *ctx, const gmle_fit_desc *desc, const float 
     CK(cudaEventCreate(&e1), "cudaEventCreate");
     Tuning best{0, 0};
     float best_ms = 1e30f;
+    // threads per block: powers of two, and for one thread per ROI also 96
+    // (three warps: two such blocks of large sCMOS ROIs fit where one of four
+    // warps does)
+    static const int kThreads[] = {32, 64, 96, 128, 256};
     for (int tpr = 1; tpr <= 8; tpr *= 2) {
-        for (int threads = 32; threads <= (tpr == 1 ? gmle::kMaxThreadsR1 : 256); threads *= 2) {
+        for (int threads : kThreads) {
+            if (threads > (tpr == 1 ? gmle::kMaxThreadsR1 : 256)) continue;
+            if (tpr > 1 && threads == 96) continue;
             const int rpb = threads / tpr;
             if (rpb < 1 || gmle::smem_bytes(desc->model, desc->box, scmos, tpr, rpb) > 227 * 1024)
                 continue;
@@ -759,11 +765,21 @@ gmle_status enqueue_table_launch(gmle_ctx *ctx, MixedSet &m, const TableLaunch &
     return GMLE_OK;
 }
 
+int plan_stream(int index, bool holds_tmem, int nf)
+{
+    // Persistent launches whose kernel holds tensor memory run in sequence on
+    // fork 0: a persistent CTA keeps its columns until its launch runs out of
+    // tiles, so a concurrent one's CTAs would wait in tcgen05.alloc on the
+    // same SMs.  The others spread over the remaining forks.
+    if (nf <= 1 || holds_tmem) return 0;
+    return 1 + index % (nf - 1);
+}
+
 gmle_status enqueue_plan(gmle_ctx *ctx, MixedSet &m, const MixedPlan &plan, cudaStream_t s)
 {
-    // All launches of a plan (plain launches of large groups, table launches
-    // of the rest) run concurrently on the fork streams, joined back into s:
-    // each launch's last, partly filled wave overlaps the others.
+    // The launches of a plan (plain launches of large groups, table launches
+    // of the rest) run concurrently on the fork streams, joined back into s,
+    // so that each launch's last, partly filled wave overlaps the others.
     const int np = (int)plan.plain.size(), nl = (int)plan.launches.size();
     const int units = np + nl;
     const bool fork = units > 1;
@@ -778,12 +794,16 @@ gmle_status enqueue_plan(gmle_ctx *ctx, MixedSet &m, const MixedPlan &plan, cuda
         const Tuning t = pick_tuning(ctx, &G.desc, G.n);
         KernelArgs a = make_args(ctx, &G.desc, G.data, G.x_corners, G.y_corners, G.n, G.params,
                                  G.crlb, G.llr, G.flags, t.tpr);
+        // plain launches are not persistent (a CTA frees its tensor memory
+        // after one tile), so they overlap freely
         CK(launch(ctx, &G.desc, a, t.rois_per_block, fork ? m.fork[u % nf] : s),
            "fit kernel launch");
     }
     for (int l = 0; l < nl; l++) {
-        const gmle_status st = enqueue_table_launch(ctx, m, plan.launches[l],
-                                                    fork ? m.fork[(np + l) % nf] : s);
+        const TableLaunch &L = plan.launches[l];
+        const bool tm = holds_tmem(L.scmos, L.shape.tpr);
+        const gmle_status st = enqueue_table_launch(
+            ctx, m, L, fork ? m.fork[plan_stream(np + l, tm, nf)] : s);
         if (st != GMLE_OK) return st;
     }
     for (int f = 0; f < nf; f++) {

@@ -288,7 +288,8 @@ struct Server {
                 }
                 for (int l = 0; l < nl; l++) {
                     const TableLaunch &L = plan.launches[l];
-                    GMLE_CK(cudaGraphLaunch(graphs[slot][L.kind].exec, nl > 1 ? m.fork[l % nf] : s),
+                    const int f = plan_stream(l, holds_tmem(L.scmos, L.shape.tpr), nf);
+                    GMLE_CK(cudaGraphLaunch(graphs[slot][L.kind].exec, nl > 1 ? m.fork[f] : s),
                             "cudaGraphLaunch");
                     ctx->launches++;
                 }
