@@ -84,6 +84,9 @@ def parse():
                    help="serving loop: ROIs per step (0: the library default)")
     p.add_argument("--max-inflight", type=int, default=0,
                    help="serving loop: concurrent steps (0: the library default)")
+    p.add_argument("--server-graphs", type=int, default=0, choices=(0, 1),
+                   help="serving loop: 1 replays a CUDA graph of persistent launches per "
+                        "kind, 0 launches one block per tile directly")
     p.add_argument("--load-rois", type=float, default=2e7,
                    help="ROIs of arrivals per load point (bounded to about 1.5 s)")
     return p.parse_args()
@@ -442,6 +445,7 @@ def run_ours(args):
         pools = loadgen.HostPools(groups)
         reqs = loadgen.make_stream(pools, n, seed=7 + rank)
         srv = serve.Server(ctx, max_inflight_steps=args.max_inflight,
+                           use_graphs=bool(args.server_graphs),
                            max_step_rois=args.max_step_rois)
         try:
             if not args.no_e2e:

@@ -26,6 +26,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <limits.h>
 #include <stdint.h>
 
 namespace gmle {
@@ -54,17 +55,21 @@ struct KernelArgs {
 
 // Group table of a table launch.  A table launch fits every group of one
 // (PSF model, box size, camera family) of a mixed batch: its groups' ROIs are
-// cut into tiles of rois_per_block ROIs, numbered group after group, and a
-// persistent grid takes tiles from `counter` (work stealing) until none is
-// left.  With `tiles`, entry t is (group << 32) | (tile index within the
-// group); without it, the tile's group is found by binary search of `tile0`
-// (first tile of each group, increasing).
+// cut into tiles of rois_per_block ROIs, numbered group after group.  With a
+// `counter`, a persistent grid takes tiles from it (work stealing) until none
+// is left; without one, the grid has one block per tile and block b fits tile
+// b, so that each block frees its resources (tensor memory included) after
+// one tile and concurrent launches interleave like plain launches.  With
+// `tiles`, entry t is (group << 32) | (tile index within the group); without
+// it, the tile's group is found by binary search of `tile0` (first tile of
+// each group, increasing).
 struct TileTable {
     const int64_t *header;        // [0] groups, [1] tiles; nullptr: plain launch
     const KernelArgs *groups;     // per group: its kernel arguments
     const int64_t *tiles;         // per tile: (group << 32) | local tile, or nullptr
     const int64_t *tile0;         // per group: first tile (used when tiles is nullptr)
-    unsigned long long *counter;  // next tile; zero when the launch starts
+    unsigned long long *counter;  // next tile, zero when the launch starts; nullptr:
+                                  // one block per tile
 };
 
 template <int MODEL> struct ModelInfo;
@@ -492,15 +497,16 @@ __device__ uint8_t crlb_from_fisher(double (&F)[P][P], float *crlb)
 // offset of each ROI's first pixel (int64), one ok flag per slot, and, when
 // several lanes share a ROI (tpr > 1), NT * BOX y-axis table entries.
 //
-// One thread per ROI (tpr == 1) with sCMOS data keeps only the data plane in
-// shared memory: each thread's variance tile lives in its tensor-memory lane
-// (TmemVar below), which halves the shared memory per resident ROI.
+// One thread per ROI (tpr == 1) keeps only the data plane in shared memory:
+// with sCMOS data each thread's variance tile lives in its tensor-memory lane
+// (TmemVar below), and its ROI's map offset and ok flag in its registers
+// (stage_r1), so a ROI takes box^2 floats.
 __host__ __device__ inline size_t smem_bytes(int model, int box, bool scmos, int tpr, int rois)
 {
+    if (tpr == 1) return (size_t)rois * sizeof(float) * box * box;
     const int nt = model == 0 ? 3 : 5;
-    const bool var_in_smem = scmos && tpr > 1;
-    return (size_t)rois * (sizeof(float) * ((size_t)box * box * (var_in_smem ? 2 : 1) +
-                                            (tpr > 1 ? (size_t)nt * box : 0)) +
+    return (size_t)rois * (sizeof(float) * ((size_t)box * box * (scmos ? 2 : 1) +
+                                            (size_t)nt * box) +
                            (scmos ? sizeof(long long) : 0) + sizeof(int));
 }
 
@@ -529,16 +535,19 @@ __device__ __forceinline__ void table_slot_init(TableSlot *ts)
     if (threadIdx.x == 0) ts->grp = -1;
 }
 
-// The block's next tile of a table launch: thread 0 takes it from the counter
+// The block's k-th tile of a table launch: thread 0 takes it from the counter
+// (or, with one block per tile, tile blockIdx.x when k == 0 and none after)
 // and finds its group; when the group changes, the block copies the group's
 // arguments into the slot.  Returns false when no tile is left.  Ends with a
 // barrier, so the slot is stable for the whole tile; the caller puts a
 // barrier between the end of a tile and the next call.
-__device__ __forceinline__ bool table_next(const TileTable &t, int R, TableSlot *ts,
+__device__ __forceinline__ bool table_next(const TileTable &t, int R, TableSlot *ts, int k,
                                            int64_t &roi0, int &nroi)
 {
     if (threadIdx.x == 0) {
-        const long long tile = (long long)atomicAdd(t.counter, 1ull);
+        const long long tile = t.counter ? (long long)atomicAdd(t.counter, 1ull)
+                               : k == 0  ? (long long)blockIdx.x
+                                         : LLONG_MAX;
         int g = -1;
         long long local = -1;
         if (tile < t.header[1]) {
@@ -714,47 +723,95 @@ __device__ __forceinline__ void adu_to_electrons(const KernelArgs &a, float *spi
     }
 }
 
-// Variance tile of this thread's ROI (slot threadIdx.x) into its TMEM lane,
-// pixel p at column p; zeros for an empty or rejected slot.  Every thread of
-// the block calls it (the stores are warp-wide).
+// Copy of the block's data plane, nroi ROIs of box^2 floats contiguous in
+// global memory from `src`, to `spix` (16-byte cp.async where the source is
+// aligned); slots [nroi, R) are zero-filled.  Waits for the thread's copies.
 template <int BOX>
-__device__ __forceinline__ void stage_var_tmem(const KernelArgs &a, const float *spix,
-                                               const int *sok, int R, int nroi, uint32_t taddr)
+__device__ __forceinline__ void copy_data_plane(float *spix, const float *src, int R, int nroi)
 {
     constexpr int B2 = BOX * BOX;
-    const long long *sbase = reinterpret_cast<const long long *>(spix + R * B2);
+    const int cnt = nroi * B2;
+    if ((reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
+        const int c4 = cnt >> 2;
+        for (int e = threadIdx.x; e < c4; e += blockDim.x) cp_async16(spix + 4 * e, src + 4 * e);
+        for (int e = (c4 << 2) + threadIdx.x; e < cnt; e += blockDim.x)
+            cp_async4(spix + e, src + e, 4);
+    } else {
+        for (int e = threadIdx.x; e < cnt; e += blockDim.x) cp_async4(spix + e, src + e, 4);
+    }
+    for (int e = cnt + threadIdx.x; e < R * B2; e += blockDim.x) spix[e] = 0.f;
+    cp_async_wait_all();
+}
+
+// Staging of the one-thread-per-ROI kernel (slot g = threadIdx.x holds ROI
+// roi0 + g).  The data plane is copied block-wide; after a barrier each thread
+// finishes its own ROI.  For sCMOS it checks the corners, gathers the ROI's
+// variance tile from the resident map into its tensor-memory lane (pixel p at
+// column p, zeros for an empty or rejected slot), and converts ADU data in
+// place, (ADU - offset) * gain (src/camera_models.jl:110-113); the gathers of
+// 16 pixels are issued before any is used.  The map offset and the ok flag
+// stay in registers, so a ROI takes only its pixels in shared memory.  Every
+// thread of the block calls it (the tensor-memory stores are warp-wide).
+// Returns whether slot g holds a ROI with valid corners.
+template <int BOX, bool SCMOS>
+__device__ __forceinline__ bool stage_r1(const KernelArgs &a, float *spix, int R, int64_t roi0,
+                                         int nroi, uint32_t taddr)
+{
+    constexpr int B2 = BOX * BOX;
+    copy_data_plane<BOX>(spix, a.data + roi0 * B2, R, nroi);
+    __syncthreads();  // other threads' copies of this thread's ROI
     const int g = threadIdx.x;
-    const bool ok = g < nroi && sok[g];
-    const long long base = ok ? sbase[g] : 0;
+    bool ok = g < nroi;
+    if (!SCMOS) return ok;
+    long long base = 0;
+    if (ok) {
+        const int32_t x0 = a.xc[roi0 + g], y0 = a.yc[roi0 + g];
+        ok = x0 >= 1 && y0 >= 1 && x0 + BOX - 1 <= a.nx && y0 + BOX - 1 <= a.ny;
+        if (!ok) atomicAdd(a.bad_corners, 1ull);
+        base = ok ? (long long)(y0 - 1) + (long long)a.ny * (long long)(x0 - 1) : 0;
+    }
+    __syncwarp();  // converged for the warp-wide stores
+    float *pix = spix + g * B2;
+    const bool adu = a.adu;  // uniform over the launch
 #pragma unroll
     for (int c = 0; c < TmemVar<BOX>::CHUNKS; c++) {
-        float v[16];
+        float v[16], off[16], gn[16];
 #pragma unroll
         for (int u = 0; u < 16; u++) {
             const int p = 16 * c + u;
             const int j = p / BOX, i = p - j * BOX;
-            v[u] = (ok && p < B2) ? __ldg(a.var + base + i + (long long)a.ny * j) : 0.f;
+            const long long m = base + i + (long long)a.ny * j;
+            const bool in = ok && p < B2;
+            v[u] = in ? __ldg(a.var + m) : 0.f;
+            off[u] = (adu && in) ? __ldg(a.offset + m) : 0.f;
+            gn[u] = (adu && in) ? __ldg(a.gain + m) : 1.f;
         }
         tmem_st16(taddr + 16 * c, v);
+        if (adu) {
+            // a rejected or empty slot converts by (x - 0) * 1: unchanged
+#pragma unroll
+            for (int u = 0; u < 16; u++) {
+                const int p = 16 * c + u;
+                if (p < B2) pix[p] = __fmul_rn(__fadd_rn(pix[p], -off[u]), gn[u]);
+            }
+        }
     }
     tmem_wait_st();
+    return ok;
 }
 
-// Stage the block's R ROIs (contiguous in global memory) into shared memory.
-// All pixel (and variance-tile) copies of a thread are issued as cp.async
-// before any is waited for; for sCMOS the variance tile is gathered from the
-// resident map and ADU data are converted, (ADU - offset) * gain
-// (src/camera_models.jl:110-113), with the gain/offset loads batched.
-//
-// With TM (sCMOS, one thread per ROI) only the data plane is staged here, with
-// the Poisson path's contiguous copies; the variance tiles go to tensor memory
-// (stage_var_tmem).
-template <int BOX, bool SCMOS, bool TM = false>
+// Stage the block's R ROIs (contiguous in global memory) into shared memory
+// for the several-lanes-per-ROI kernel.  All pixel (and variance-tile) copies
+// of a thread are issued as cp.async before any is waited for; for sCMOS the
+// variance tile is gathered from the resident map and ADU data are converted,
+// (ADU - offset) * gain (src/camera_models.jl:110-113), with the gain/offset
+// loads batched.
+template <int BOX, bool SCMOS>
 __device__ __forceinline__ void stage_block(const KernelArgs &a, float *spix, int *sok, int R,
                                             int64_t roi0, int nroi)
 {
     constexpr int B2 = BOX * BOX;
-    constexpr int PS = (SCMOS && !TM) ? 2 : 1;  // floats per staged pixel
+    constexpr int PS = SCMOS ? 2 : 1;  // floats per staged pixel
     long long *sbase = reinterpret_cast<long long *>(spix + R * B2 * PS);
     for (int g = threadIdx.x; g < R; g += blockDim.x) {
         int ok = g < nroi;
@@ -770,22 +827,8 @@ __device__ __forceinline__ void stage_block(const KernelArgs &a, float *spix, in
     }
     const float *src = a.data + roi0 * B2;
     const int cnt = nroi * B2;
-    if (!SCMOS || TM) {
-        if ((reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
-            const int c4 = cnt >> 2;
-            for (int e = threadIdx.x; e < c4; e += blockDim.x)
-                cp_async16(spix + 4 * e, src + 4 * e);
-            for (int e = (c4 << 2) + threadIdx.x; e < cnt; e += blockDim.x)
-                cp_async4(spix + e, src + e, 4);
-        } else {
-            for (int e = threadIdx.x; e < cnt; e += blockDim.x) cp_async4(spix + e, src + e, 4);
-        }
-        for (int e = cnt + threadIdx.x; e < R * B2; e += blockDim.x) spix[e] = 0.f;
-        cp_async_wait_all();
-        if (SCMOS && a.adu) {
-            __syncthreads();  // the copies of other threads, sok and sbase
-            adu_to_electrons<BOX, 1>(a, spix, sok, sbase, cnt);
-        }
+    if (!SCMOS) {
+        copy_data_plane<BOX>(spix, src, R, nroi);
     } else {
         __syncthreads();  // sok, sbase
         // consecutive e walk down a column: contiguous map addresses
@@ -1044,13 +1087,10 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
 
     const int R = blockDim.x;
     float *spix = smem;
-    int *sok = reinterpret_cast<int *>(spix + R * B2 + (SCMOS ? 2 * R : 0));
-    stage_block<BOX, SCMOS, true>(a, spix, sok, R, roi0, nroi);
-    if (SCMOS) stage_var_tmem<BOX>(a, spix, sok, R, nroi, taddr);
+    const bool valid = stage_r1<BOX, SCMOS>(a, spix, R, roi0, nroi, taddr);
 
     const int g = threadIdx.x;
     if (__all_sync(0xffffffffu, g >= nroi)) return;
-    const bool valid = g < nroi && sok[g];
     const float *pix = spix + g * B2 * PS;
 
     float th[P];
@@ -1202,7 +1242,7 @@ __global__ void __launch_bounds__(128) fit_kernel_r1(const KernelArgs a, const T
         table_slot_init(ts);
         int64_t roi0;
         int nroi;
-        while (table_next(t, R, ts, roi0, nroi)) {
+        for (int k = 0; table_next(t, R, ts, k, roi0, nroi); k++) {
             fit_rois_r1<MODEL, BOX, SCMOS>(ts->a, roi0, nroi, smem, taddr);
             __syncthreads();  // the tile's shared memory and slot are free again
         }
@@ -1413,7 +1453,7 @@ __global__ void __launch_bounds__(256) fit_kernel(const KernelArgs a, const Tile
     table_slot_init(ts);
     int64_t roi0;
     int nroi;
-    while (table_next(t, R, ts, roi0, nroi)) {
+    for (int k = 0; table_next(t, R, ts, k, roi0, nroi); k++) {
         fit_rois_tpr<MODEL, BOX, SCMOS>(ts->a, roi0, nroi, smem);
         __syncthreads();  // the tile's shared memory and slot are free again
     }

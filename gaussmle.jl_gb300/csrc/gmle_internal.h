@@ -89,6 +89,7 @@ struct MixedSet {
 struct TableLaunch {
     int kind = -1, model = 0, box = 0;
     bool scmos = false;
+    bool persistent = true;  // false: one block per tile (no tile counter)
     gmle::LaunchShape shape{};
     int64_t groups = 0, tiles = 0;
 };
@@ -145,6 +146,10 @@ void free_mixed_set(MixedSet &m);
 struct PlanOptions {
     bool allow_plain = true;
     int64_t shape_rois = 0;
+    // persistent table launches (a grid of resident blocks that take tiles from
+    // a counter; full_grid: sized for the GPU whatever the tiles) or one block
+    // per tile
+    bool persistent = true;
     bool full_grid = false;
     // table capacity to reserve: groups, and tiles for this many ROIs
     int64_t reserve_groups = 0, reserve_rois = 0;

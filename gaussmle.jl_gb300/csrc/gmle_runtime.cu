@@ -720,7 +720,10 @@ gmle_status plan_mixed(gmle_ctx *ctx, const gmle_group *groups, int32_t ngroups,
                         L.model, L.box, t.tpr, rpb, bps < 0 ? ": " : "",
                         bps < 0 ? cudaGetErrorString((cudaError_t)-bps) : "");
         const int64_t full = (int64_t)ctx->num_sms * bps;
-        L.shape = gmle::LaunchShape{t.tpr, rpb, opt.full_grid ? full : std::min(full, tiles)};
+        L.persistent = opt.persistent;
+        L.shape = gmle::LaunchShape{t.tpr, rpb, !opt.persistent ? tiles
+                                                : opt.full_grid ? full
+                                                                : std::min(full, tiles)};
         L.groups = hdr[0];
         L.tiles = tiles;
         plan.launches.push_back(L);
@@ -754,11 +757,12 @@ gmle_status enqueue_table_launch(gmle_ctx *ctx, MixedSet &m, const TableLaunch &
     t.groups = reinterpret_cast<const KernelArgs *>(base + kTableHeader);
     t.tiles = reinterpret_cast<const int64_t *>(base + b.tiles_off());
     t.tile0 = nullptr;
-    t.counter = b.d_counter;
+    t.counter = L.persistent ? b.d_counter : nullptr;
     KernelArgs a;
     std::memset(&a, 0, sizeof a);
     a.tpr = L.shape.tpr;
-    CK(cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned long long), q), "reset tile counter");
+    if (L.persistent)
+        CK(cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned long long), q), "reset tile counter");
     ctx->launches++;
     CK(gmle::launch_fit(L.model, L.box, L.scmos, a, t, L.shape, q), "table launch");
     if (!m.zero_copy) CK(cudaEventRecord(b.used, q), "cudaEventRecord");
@@ -801,7 +805,7 @@ gmle_status enqueue_plan(gmle_ctx *ctx, MixedSet &m, const MixedPlan &plan, cuda
     }
     for (int l = 0; l < nl; l++) {
         const TableLaunch &L = plan.launches[l];
-        const bool tm = holds_tmem(L.scmos, L.shape.tpr);
+        const bool tm = L.persistent && holds_tmem(L.scmos, L.shape.tpr);
         const gmle_status st = enqueue_table_launch(
             ctx, m, L, fork ? m.fork[plan_stream(np + l, tm, nf)] : s);
         if (st != GMLE_OK) return st;

@@ -7,11 +7,15 @@
 //              in on the input stream                        (admission by HBM)
 //   step    -> every admitted request whose copy has landed joins the next
 //              step: one persistent table launch per (camera family, model,
-//              box) present; up to max_inflight_steps steps run concurrently
-//              on their own streams, each kind's launch a replay of a CUDA
-//              graph captured once per (slot, kind)        (continuous batching)
+//              box) present; up to max_inflight_steps steps run concurrently,
+//              their launches spread over a few run streams: one block per
+//              tile, or a replay of a CUDA graph of a persistent launch
+//              captured once per (slot, kind)               (continuous batching)
 //   drain   -> results copied out on the output stream, memory released,
 //              waiters woken; the latency submit -> results-on-host recorded.
+//              Outputs in pinned (page-locked) host memory are written by the
+//              kernels themselves over the host link, so such a request is
+//              done when its step is: no copy-out call and no output stream.
 // The scheduler never waits on the GPU: it polls events and sleeps briefly when
 // nothing progressed, and no kernel waits on the host.
 #include <cuda_runtime.h>
@@ -35,6 +39,11 @@ namespace {
 using Clock = std::chrono::steady_clock;
 
 constexpr int kMaxSlots = 8;
+// Streams that run the steps' launches.  With the input and output streams
+// they are 8, the number of hardware work queues a CUDA context has by
+// default (CUDA_DEVICE_MAX_CONNECTIONS): more streams would share queues, and
+// a launch could then wait behind an unrelated one.
+constexpr int kRunStreams = 6;
 constexpr int kServerTableCap = 4096;  // groups (requests) per step and kind
 
 enum ReqState { PENDING, STAGED, RUNNING, DRAINING, DONE, FAILED };
@@ -45,6 +54,10 @@ struct Request {
     uint64_t ticket = 0;
     gmle_group host{};   // caller's descriptor and host pointers
     gmle_group dev{};    // the same with device pointers into the arena
+    // outputs written in place: device addresses of the caller's pinned
+    // params, crlb, llr, flags (all pinned, or the request copies them out)
+    bool direct_out = false;
+    void *out_dev[4] = {};
     int64_t off = -1, bytes = 0;
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
     Clock::time_point t_submit, t_done;
@@ -93,7 +106,7 @@ struct Arena {
 
 struct Step {
     int slot = -1;
-    cudaEvent_t done = nullptr;
+    std::vector<cudaEvent_t> done;  // one per launch, recorded after it (the slot's)
     std::vector<Request *> reqs;
 };
 
@@ -115,8 +128,12 @@ struct Server {
     std::vector<cudaEvent_t> event_pool;
     Arena arena;
     cudaStream_t s_in = nullptr, s_out = nullptr;
-    cudaStream_t s_step[kMaxSlots] = {};
-    cudaEvent_t step_done[kMaxSlots] = {};
+    cudaStream_t s_run[kRunStreams] = {};
+    cudaStream_t s_capture = nullptr;  // graph capture only: never runs work
+    int next_run = 0;
+    // per slot and kind: the event after that kind's launch (scheduler thread
+    // only, created on first use; a slot's step has at most one launch per kind)
+    cudaEvent_t launch_done[kMaxSlots][kKinds] = {};
     bool slot_busy[kMaxSlots] = {};
     MixedSet sets[kMaxSlots];
     // per slot and kind: the captured counter reset + table launch, and the
@@ -148,11 +165,12 @@ struct Server {
         if (e) event_pool.push_back(e);
     }
 
-    int64_t footprint(const gmle_group &g) const
+    static int64_t footprint(const gmle_group &g, bool direct_out)
     {
         const int64_t n = g.n, b2 = (int64_t)g.desc.box * g.desc.box;
         const int P = nparams(g.desc.model);
-        int64_t b = align256(4 * n * b2) + 2 * align256(4 * n * P) + align256(4 * n) + align256(n);
+        int64_t b = align256(4 * n * b2);
+        if (!direct_out) b += 2 * align256(4 * n * P) + align256(4 * n) + align256(n);
         if (g.desc.camera != GMLE_CAMERA_POISSON) b += 2 * align256(4 * n);
         return b;
     }
@@ -165,14 +183,21 @@ struct Server {
         r->dev = r->host;
         r->dev.data = reinterpret_cast<float *>(p);
         p += align256(4 * n * b2);
-        r->dev.params = reinterpret_cast<float *>(p);
-        p += align256(4 * n * P);
-        r->dev.crlb = reinterpret_cast<float *>(p);
-        p += align256(4 * n * P);
-        r->dev.llr = reinterpret_cast<float *>(p);
-        p += align256(4 * n);
-        r->dev.flags = reinterpret_cast<uint8_t *>(p);
-        p += align256(n);
+        if (r->direct_out) {
+            r->dev.params = static_cast<float *>(r->out_dev[0]);
+            r->dev.crlb = static_cast<float *>(r->out_dev[1]);
+            r->dev.llr = static_cast<float *>(r->out_dev[2]);
+            r->dev.flags = static_cast<uint8_t *>(r->out_dev[3]);
+        } else {
+            r->dev.params = reinterpret_cast<float *>(p);
+            p += align256(4 * n * P);
+            r->dev.crlb = reinterpret_cast<float *>(p);
+            p += align256(4 * n * P);
+            r->dev.llr = reinterpret_cast<float *>(p);
+            p += align256(4 * n);
+            r->dev.flags = reinterpret_cast<uint8_t *>(p);
+            p += align256(n);
+        }
         if (r->host.desc.camera != GMLE_CAMERA_POISSON) {
             r->dev.x_corners = reinterpret_cast<int32_t *>(p);
             p += align256(4 * n);
@@ -180,6 +205,21 @@ struct Server {
         } else {
             r->dev.x_corners = r->dev.y_corners = nullptr;
         }
+    }
+
+    // Results on the host: memory released, waiters woken (lock held).
+    void complete(Request *r)
+    {
+        r->t_done = Clock::now();
+        r->state = DONE;
+        arena.release(r->off, r->bytes);
+        r->off = -1;
+        completed++;
+        rois_done += r->host.n;
+        last_done = r->t_done;
+        if (lat_ms.size() < (1u << 22))
+            lat_ms.push_back(std::chrono::duration<float, std::milli>(r->t_done - r->t_submit).count());
+        cv_done.notify_all();
     }
 
     void fail_request(Request *r, gmle_status st)
@@ -226,49 +266,60 @@ struct Server {
     }
 
     // One step: the tables of every kind in the slot's pinned buffers (read
-    // in place by the kernels), then per kind present a replay of the slot's
-    // graph for that kind (captured on first use, or again after its shape or
-    // table changed), the kinds concurrently on the slot's fork streams.
-    // Shapes come from the tuning for a full step and grids are full, so each
-    // (slot, kind) is captured once: no capture stalls the loop once every
-    // kind has been seen.
-    gmle_status launch_step(int slot, const std::vector<Request *> &reqs)
+    // in place by the kernels), then one launch per kind present, spread over
+    // the run streams, each followed by an event in `done`.  Direct launches
+    // have one block per tile.  With graphs, each launch is a replay of the
+    // slot's graph of a persistent launch for that kind (captured on first
+    // use, or again after its shape or table changed); shapes come from the
+    // tuning for a full step and grids are full, so each (slot, kind) is
+    // captured once.  Persistent launches that hold tensor memory run in
+    // sequence on the first run stream.
+    gmle_status launch_step(int slot, const std::vector<Request *> &reqs,
+                            std::vector<cudaEvent_t> &done)
     {
         std::vector<gmle_group> groups;
         groups.reserve(reqs.size());
         for (Request *r : reqs) groups.push_back(r->dev);
         MixedSet &m = sets[slot];
         MixedPlan plan;
-        cudaStream_t s = s_step[slot];
-        {
-            std::lock_guard<std::mutex> lk(ctx->mu);
-            PlanOptions opt;
-            opt.allow_plain = false;
-            opt.shape_rois = cfg.max_step_rois;
-            opt.full_grid = true;
-            opt.reserve_groups = kServerTableCap;
-            opt.reserve_rois = cfg.max_step_rois;
-            gmle_status st = plan_mixed(ctx, groups.data(), (int32_t)groups.size(), m, plan, opt);
-            if (st != GMLE_OK) return st;
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        PlanOptions opt;
+        opt.allow_plain = false;
+        opt.shape_rois = cfg.max_step_rois;
+        // a graph replays a fixed grid: persistent launches; direct launches
+        // take one block per tile
+        opt.persistent = cfg.use_graphs != 0;
+        opt.full_grid = true;
+        opt.reserve_groups = kServerTableCap;
+        opt.reserve_rois = cfg.max_step_rois;
+        gmle_status st = plan_mixed(ctx, groups.data(), (int32_t)groups.size(), m, plan, opt);
+        if (st != GMLE_OK) return st;
+        for (const TableLaunch &L : plan.launches) {
+            cudaStream_t q;
+            if (L.persistent && holds_tmem(L.scmos, L.shape.tpr))
+                q = s_run[0];
+            else if (L.persistent)
+                q = s_run[1 + next_run++ % (kRunStreams - 1)];
+            else
+                q = s_run[next_run++ % kRunStreams];
             if (!cfg.use_graphs) {
-                st = enqueue_plan(ctx, m, plan, s);
+                st = enqueue_table_launch(ctx, m, L, q);
                 if (st != GMLE_OK) return st;
             } else {
-                for (const TableLaunch &L : plan.launches) {
-                    const TableBufs &b = m.tables[L.kind];
-                    const std::vector<int64_t> key = {L.shape.tpr, L.shape.rois_per_block,
-                                                      L.shape.grid, (int64_t)(uintptr_t)b.h_base,
-                                                      b.cap_groups};
-                    KindGraph &kg = graphs[slot][L.kind];
-                    if (kg.exec && kg.key == key) continue;
+                const TableBufs &b = m.tables[L.kind];
+                const std::vector<int64_t> key = {L.shape.tpr, L.shape.rois_per_block,
+                                                  L.shape.grid, (int64_t)(uintptr_t)b.h_base,
+                                                  b.cap_groups};
+                KindGraph &kg = graphs[slot][L.kind];
+                if (!kg.exec || kg.key != key) {
                     if (kg.exec) cudaGraphExecDestroy(kg.exec);
                     kg.exec = nullptr;
                     cudaGraph_t g = nullptr;
-                    GMLE_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal),
+                    GMLE_CK(cudaStreamBeginCapture(s_capture, cudaStreamCaptureModeThreadLocal),
                             "cudaStreamBeginCapture");
-                    st = enqueue_table_launch(ctx, m, L, s);
+                    st = enqueue_table_launch(ctx, m, L, s_capture);
                     ctx->launches--;  // counted when the graph is launched
-                    const cudaError_t e = cudaStreamEndCapture(s, &g);
+                    const cudaError_t e = cudaStreamEndCapture(s_capture, &g);
                     if (st != GMLE_OK) {
                         if (g) cudaGraphDestroy(g);
                         return st;
@@ -279,27 +330,14 @@ struct Server {
                     GMLE_CK(e2, "cudaGraphInstantiate");
                     kg.key = key;
                 }
-                const int nl = (int)plan.launches.size();
-                const int nf = std::min(nl, kForks);
-                if (nl > 1) {
-                    GMLE_CK(cudaEventRecord(m.ev_fork, s), "cudaEventRecord");
-                    for (int f = 0; f < nf; f++)
-                        GMLE_CK(cudaStreamWaitEvent(m.fork[f], m.ev_fork, 0), "cudaStreamWaitEvent");
-                }
-                for (int l = 0; l < nl; l++) {
-                    const TableLaunch &L = plan.launches[l];
-                    const int f = plan_stream(l, holds_tmem(L.scmos, L.shape.tpr), nf);
-                    GMLE_CK(cudaGraphLaunch(graphs[slot][L.kind].exec, nl > 1 ? m.fork[f] : s),
-                            "cudaGraphLaunch");
-                    ctx->launches++;
-                }
-                for (int f = 0; nl > 1 && f < nf; f++) {
-                    GMLE_CK(cudaEventRecord(m.ev_join[f], m.fork[f]), "cudaEventRecord");
-                    GMLE_CK(cudaStreamWaitEvent(s, m.ev_join[f], 0), "cudaStreamWaitEvent");
-                }
+                GMLE_CK(cudaGraphLaunch(kg.exec, q), "cudaGraphLaunch");
+                ctx->launches++;
             }
+            cudaEvent_t &ev = launch_done[slot][L.kind];
+            if (!ev) GMLE_CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
+            GMLE_CK(cudaEventRecord(ev, q), "cudaEventRecord");
+            done.push_back(ev);
         }
-        GMLE_CK(cudaEventRecord(step_done[slot], s), "cudaEventRecord");
         return GMLE_OK;
     }
 
@@ -338,31 +376,36 @@ struct Server {
                 std::vector<Request *> step;
                 int64_t rois = 0;
                 int ngroups = 0;
-                for (auto it = staged.begin(); it != staged.end();) {
+                // the input copies run in order on one stream: the first one
+                // still in flight ends the search
+                size_t taken = 0;
+                for (; taken < staged.size(); taken++) {
+                    Request *r = staged[taken];
                     if (rois >= cfg.max_step_rois || ngroups >= kServerTableCap) break;
-                    if (cudaEventQuery((*it)->ev_in) == cudaSuccess) {
-                        rois += (*it)->host.n;
-                        ngroups++;
-                        (*it)->state = RUNNING;
-                        step.push_back(*it);
-                        it = staged.erase(it);
-                    } else {
-                        ++it;
-                    }
+                    if (cudaEventQuery(r->ev_in) != cudaSuccess) break;
+                    rois += r->host.n;
+                    ngroups++;
+                    r->state = RUNNING;
+                    step.push_back(r);
                 }
+                staged.erase(staged.begin(), staged.begin() + taken);
                 if (!step.empty()) {
                     slot_busy[slot] = true;
+                    std::vector<cudaEvent_t> done;
                     lk.unlock();
-                    const gmle_status st = launch_step(slot, step);
+                    const gmle_status st = launch_step(slot, step, done);
                     lk.lock();
                     if (st != GMLE_OK) {
+                        // launches already enqueued still read the slot's
+                        // tables and the requests' memory: wait for them
+                        for (cudaEvent_t e : done) cudaEventSynchronize(e);
                         for (Request *r : step) fail_request(r, st);
                         slot_busy[slot] = false;
                     } else {
                         steps++;
                         Step s;
                         s.slot = slot;
-                        s.done = step_done[slot];
+                        s.done = std::move(done);
                         s.reqs = std::move(step);
                         inflight.push_back(std::move(s));
                     }
@@ -371,7 +414,10 @@ struct Server {
             }
             // 3. finished launches: copy results out
             for (auto it = inflight.begin(); it != inflight.end();) {
-                if (cudaEventQuery(it->done) != cudaSuccess) {
+                bool finished = true;
+                for (cudaEvent_t e : it->done)
+                    if (cudaEventQuery(e) != cudaSuccess) { finished = false; break; }
+                if (!finished) {
                     ++it;
                     continue;
                 }
@@ -380,11 +426,13 @@ struct Server {
                 it = inflight.erase(it);
                 lk.unlock();
                 std::vector<cudaError_t> errs;
-                for (Request *r : reqs) errs.push_back(issue_out(r));
+                for (Request *r : reqs) errs.push_back(r->direct_out ? cudaSuccess : issue_out(r));
                 lk.lock();
                 for (size_t q = 0; q < reqs.size(); q++) {
                     if (errs[q] != cudaSuccess) {
                         fail_request(reqs[q], GMLE_CUDA_ERROR);
+                    } else if (reqs[q]->direct_out) {
+                        complete(reqs[q]);  // the kernels wrote the results in place
                     } else {
                         reqs[q]->state = DRAINING;
                         draining.push_back(reqs[q]);
@@ -400,17 +448,7 @@ struct Server {
                     continue;
                 }
                 it = draining.erase(it);
-                r->t_done = Clock::now();
-                r->state = DONE;
-                arena.release(r->off, r->bytes);
-                r->off = -1;
-                completed++;
-                rois_done += r->host.n;
-                last_done = r->t_done;
-                if (lat_ms.size() < (1u << 22))
-                    lat_ms.push_back(
-                        std::chrono::duration<float, std::milli>(r->t_done - r->t_submit).count());
-                cv_done.notify_all();
+                complete(r);
                 progress = true;
             }
             const bool busy = !pending.empty() || !staged.empty() || !inflight.empty() ||
@@ -440,14 +478,18 @@ void server_destroy(gmle_ctx *ctx)
     S->cv_work.notify_all();
     if (S->th.joinable()) S->th.join();
     cudaSetDevice(ctx->device);
+    for (int k = 0; k < kRunStreams; k++)
+        if (S->s_run[k]) cudaStreamSynchronize(S->s_run[k]);
     for (int k = 0; k < kMaxSlots; k++) {
-        if (S->s_step[k]) cudaStreamSynchronize(S->s_step[k]);
         for (auto &g : S->graphs[k])
             if (g.exec) cudaGraphExecDestroy(g.exec);
+        for (cudaEvent_t e : S->launch_done[k])
+            if (e) cudaEventDestroy(e);
         free_mixed_set(S->sets[k]);
-        if (S->s_step[k]) cudaStreamDestroy(S->s_step[k]);
-        if (S->step_done[k]) cudaEventDestroy(S->step_done[k]);
     }
+    for (int k = 0; k < kRunStreams; k++)
+        if (S->s_run[k]) cudaStreamDestroy(S->s_run[k]);
+    if (S->s_capture) cudaStreamDestroy(S->s_capture);
     if (S->s_in) cudaStreamDestroy(S->s_in);
     if (S->s_out) cudaStreamDestroy(S->s_out);
     for (auto &kv : S->table) {
@@ -474,12 +516,8 @@ gmle_status gmle_server_start(gmle_ctx *ctx, const gmle_server_config *config)
     cudaSetDevice(ctx->device);
     Server *S = new Server();
     S->ctx = ctx;
-    if (config) {
-        S->cfg = *config;
-    } else {
-        S->cfg.use_graphs = 1;
-    }
-    if (S->cfg.max_inflight_steps <= 0) S->cfg.max_inflight_steps = 4;
+    if (config) S->cfg = *config;
+    if (S->cfg.max_inflight_steps <= 0) S->cfg.max_inflight_steps = 8;
     S->cfg.max_inflight_steps = std::min(S->cfg.max_inflight_steps, kMaxSlots);
     if (S->cfg.max_step_rois <= 0) S->cfg.max_step_rois = 1ll << 21;
     if (S->cfg.max_pending <= 0) S->cfg.max_pending = 1 << 16;
@@ -505,13 +543,12 @@ gmle_status gmle_server_start(gmle_ctx *ctx, const gmle_server_config *config)
     S->arena.size = budget;
     S->arena.free_[0] = budget;
     bool ok = cudaStreamCreateWithFlags(&S->s_in, cudaStreamNonBlocking) == cudaSuccess &&
-              cudaStreamCreateWithFlags(&S->s_out, cudaStreamNonBlocking) == cudaSuccess;
-    for (int k = 0; ok && k < S->cfg.max_inflight_steps; k++) {
-        ok = cudaStreamCreateWithFlags(&S->s_step[k], cudaStreamNonBlocking) == cudaSuccess &&
-             cudaEventCreateWithFlags(&S->step_done[k], cudaEventDisableTiming) == cudaSuccess;
-        ok = ok && init_mixed_set(ctx, S->sets[k]) == GMLE_OK;
-        S->sets[k].zero_copy = true;
-    }
+              cudaStreamCreateWithFlags(&S->s_out, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&S->s_capture, cudaStreamNonBlocking) == cudaSuccess;
+    for (int k = 0; ok && k < kRunStreams; k++)
+        ok = cudaStreamCreateWithFlags(&S->s_run[k], cudaStreamNonBlocking) == cudaSuccess;
+    // a slot's tables are pinned host memory read in place by its launches
+    for (int k = 0; k < S->cfg.max_inflight_steps; k++) S->sets[k].zero_copy = true;
     ctx->server = S;
     if (!ok) {
         server_destroy(ctx);
@@ -550,18 +587,32 @@ gmle_status gmle_submit(gmle_ctx *ctx, const gmle_group *request, uint64_t *tick
     }
     Request *r = new Request();
     r->host = *request;
-    r->bytes = S->footprint(*request);
+    // outputs in pinned host memory are written in place by the kernels
+    const void *outs[4] = {request->params, request->crlb, request->llr, request->flags};
+    r->direct_out = true;
+    for (int k = 0; k < 4 && r->direct_out; k++) {
+        if (!outs[k]) continue;  // flags are optional
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, outs[k]) != cudaSuccess) {
+            cudaGetLastError();
+            r->direct_out = false;
+        } else {
+            r->direct_out = at.type == cudaMemoryTypeHost && at.devicePointer != nullptr;
+            r->out_dev[k] = at.devicePointer;
+        }
+    }
+    r->bytes = Server::footprint(*request, r->direct_out);
     r->t_submit = Clock::now();
     {
         std::lock_guard<std::mutex> lk(S->mu);
         if (r->bytes > S->arena.size || (int64_t)S->pending.size() >= S->cfg.max_pending) {
             S->rejected++;
+            const long long need = (long long)r->bytes;
             delete r;
             std::lock_guard<std::mutex> lk2(ctx->mu);
             return fail(ctx, GMLE_ADMISSION_REJECTED,
                         "request of %lld ROIs needs %lld bytes; arena %lld, queue %zu",
-                        (long long)request->n, (long long)S->footprint(*request),
-                        (long long)S->arena.size, S->pending.size());
+                        (long long)request->n, need, (long long)S->arena.size, S->pending.size());
         }
         r->ev_in = S->get_event();
         r->ev_out = S->get_event();

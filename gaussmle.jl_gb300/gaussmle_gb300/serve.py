@@ -1,10 +1,12 @@
 """Mixed batches and the serving loop from Python (over the C ABI).
 
-MixedBatch: groups of device-resident ROIs fitted by one persistent,
-work-stealing kernel launch (gmle_fit_mixed_device).
+fit_mixed_device: groups of device-resident ROIs of any (model, box), one
+table launch per kind present (gmle_fit_mixed_device).
 Server: the context's request loop (gmle_server_start / gmle_submit /
 gmle_wait): admission by HBM budget, continuous batching of requests into
-persistent launches, CUDA-graph submission, p50/p99 latency.
+steps of one-block-per-tile table launches (or, with use_graphs, replays of
+CUDA graphs of persistent launches), results written in place into pinned
+host outputs, p50/p99 latency.
 """
 from __future__ import annotations
 
@@ -55,8 +57,8 @@ class Server:
     """The context's serving loop.  Host buffers passed to submit() must stay
     alive until the request is waited for."""
 
-    def __init__(self, ctx: _lib.Context, hbm_budget_bytes: int = 0, max_inflight_steps: int = 4,
-                 max_step_rois: int = 0, max_pending: int = 0, use_graphs: bool = True):
+    def __init__(self, ctx: _lib.Context, hbm_budget_bytes: int = 0, max_inflight_steps: int = 0,
+                 max_step_rois: int = 0, max_pending: int = 0, use_graphs: bool = False):
         self.ctx = ctx
         cfg = _lib.ServerConfig(hbm_budget_bytes, max_inflight_steps, max_step_rois,
                                 max_pending, int(use_graphs))

@@ -292,18 +292,23 @@ gmle_status gmle_fit_mixed_device_noalloc(const gmle_group *groups, int32_t ngro
  * per batch, src/interface.jl:220-262).  A scheduler thread owned by the
  * context admits submitted requests into a device arena (admission by HBM
  * budget, FIFO), copies their ROIs in, and continuously batches every request
- * whose data has arrived into the next persistent mixed-batch launch; up to
- * max_inflight_steps launches run concurrently, so requests that arrive while
- * others are on the GPU start as soon as SMs and memory free up.  Results are
- * copied back into the caller's host buffers, which must stay valid until
- * the request completes.
+ * whose data has arrived into the next step: one table launch per (camera
+ * family, model, box) present, with one block per tile of 32..128 ROIs.  Up
+ * to max_inflight_steps steps run concurrently, and their blocks interleave
+ * on the SMs, so requests that arrive while others are on the GPU start as
+ * soon as SMs and memory free up.  Results land in the caller's host
+ * buffers, which must stay valid until the request completes: outputs in
+ * pinned (page-locked) memory are written there by the kernels, others are
+ * copied back after the step.
  */
 typedef struct {
     int64_t hbm_budget_bytes;   /* device arena; 0 = half of the free HBM at start */
-    int32_t max_inflight_steps; /* concurrent launch steps; 0 = 4 */
-    int64_t max_step_rois;      /* ROIs per launch; 0 = 2^21 */
+    int32_t max_inflight_steps; /* concurrent steps; 0 = 8 (at most 8) */
+    int64_t max_step_rois;      /* ROIs per step; 0 = 2^21 */
     int32_t max_pending;        /* queued requests before submit rejects; 0 = 1 << 16 */
-    int32_t use_graphs;         /* 1: each launch is a replay of a captured CUDA graph */
+    int32_t use_graphs;         /* 1: each launch is a replay of a captured CUDA graph of a
+                                   persistent launch (fixed grid, blocks take tiles from a
+                                   counter); 0 (default): direct launches, one block per tile */
 } gmle_server_config;
 
 typedef struct {

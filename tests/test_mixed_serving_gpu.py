@@ -145,10 +145,13 @@ def _group(w, b):
                             b["params"], b["crlb"], b["llr"], b["flags"])
 
 
-def test_served_results_same_alone_and_in_mix(ctx):
+@pytest.mark.parametrize("graphs", [True, False], ids=["graph-replays", "block-per-tile"])
+def test_served_results_same_alone_and_in_mix(ctx, graphs):
+    """Graph replays run persistent table launches; direct launches run one
+    block per tile: both give the plain kernel's results."""
     ws = _cases()
     _set_maps(ctx, ws[0].maps)
-    srv = serve.Server(ctx, hbm_budget_bytes=256 << 20, max_inflight_steps=2)
+    srv = serve.Server(ctx, hbm_budget_bytes=256 << 20, max_inflight_steps=2, use_graphs=graphs)
     try:
         # alone: one request at a time
         alone = []
@@ -210,3 +213,72 @@ def test_admission_by_hbm_budget(ctx):
         del big
     finally:
         srv.stop()
+
+
+@pytest.mark.parametrize("pinned", [False, True], ids=["copied-out", "written-in-place"])
+@pytest.mark.parametrize("graphs", [True, False], ids=["graph-replays", "block-per-tile"])
+def test_many_requests_from_threads(ctx, graphs, pinned):
+    """400 small requests submitted and waited for from four threads at once
+    (ctypes releases the GIL, so the library sees concurrent calls): each
+    slice's results equal those of the same ROIs served as one request.
+    Outputs in pageable memory are copied out; outputs in pinned memory are
+    written in place by the kernels."""
+    import threading
+    torch = pytest.importorskip("torch")
+
+    def out(shape, dtype, fill):
+        if not pinned:
+            return np.full(shape, fill, dtype)
+        t = torch.empty(shape, dtype=torch.uint8 if dtype == np.uint8 else torch.float32,
+                        pin_memory=True)
+        t.fill_(fill)
+        return t.numpy()  # shares the pinned memory
+
+    ws = _cases()
+    _set_maps(ctx, ws[0].maps)
+    w = ws[0]
+    srv = serve.Server(ctx, hbm_budget_bytes=256 << 20, use_graphs=graphs)
+    try:
+        whole = _host_bufs(w)
+        srv.wait(srv.submit(_group(w, whole), keep=whole), timeout_s=60)
+        rng = np.random.default_rng(17)
+        slices = []
+        for _ in range(400):
+            lo = int(rng.integers(0, w.n - 1))
+            hi = int(min(w.n, lo + rng.integers(1, 121)))
+            slices.append((lo, hi))
+        outs = [None] * len(slices)
+        errors = []
+
+        def worker(part):
+            try:
+                tickets = []
+                for q in part:
+                    lo, hi = slices[q]
+                    b = {"data": np.asfortranarray(w.data[:, :, lo:hi]),
+                         "xc": w.x_corners[lo:hi].copy(), "yc": w.y_corners[lo:hi].copy(),
+                         "params": out((hi - lo, w.psf.nparams), np.float32, np.nan),
+                         "crlb": out((hi - lo, w.psf.nparams), np.float32, np.nan),
+                         "llr": out((hi - lo,), np.float32, np.nan),
+                         "flags": out((hi - lo,), np.uint8, 0)}
+                    outs[q] = b
+                    tickets.append(srv.submit(_group(w, b), keep=b))
+                for t in tickets:
+                    srv.wait(t, timeout_s=120)
+            except Exception as e:  # reported below
+                errors.append(e)
+
+        threads = [threading.Thread(target=worker, args=(list(range(k, len(slices), 4)),))
+                   for k in range(4)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        assert not errors, errors
+        st = srv.stats()
+    finally:
+        srv.stop()
+    assert st["failed"] == 0 and st["completed"] == len(slices) + 1
+    for (lo, hi), b in zip(slices, outs):
+        for key in ("params", "crlb", "llr", "flags"):
+            assert np.array_equal(b[key], whole[key][lo:hi], equal_nan=True), (lo, hi, key)
