@@ -654,14 +654,18 @@ __device__ __forceinline__ void tmem_sync()
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
+// The tensor-memory load and store touch only registers and tensor memory, so
+// they carry no "memory" clobber: global and shared accesses may move across
+// them (the gathers of the next column ahead of this column's store, the
+// pixel loads of a column ahead of its variance load).  Being volatile, they
+// keep their order among themselves and with the fences and barriers.
 __device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16])
 {
     asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, "
                  "%8, %9, %10, %11, %12, %13, %14, %15, %16};"
                  :: "r"(taddr), "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]),
                     "f"(v[6]), "f"(v[7]), "f"(v[8]), "f"(v[9]), "f"(v[10]), "f"(v[11]),
-                    "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15])
-                 : "memory");
+                    "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15]));
 }
 __device__ __forceinline__ void tmem_wait_st()
 {
@@ -678,7 +682,7 @@ __device__ __forceinline__ void tmem_ld(uint32_t taddr, float (&v)[LW])
                      : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]),
                        "=f"(v[6]), "=f"(v[7]), "=f"(v[8]), "=f"(v[9]), "=f"(v[10]), "=f"(v[11]),
                        "=f"(v[12]), "=f"(v[13]), "=f"(v[14]), "=f"(v[15])
-                     : "r"(taddr) : "memory");
+                     : "r"(taddr));
     } else {
         static_assert(LW == 8, "8 or 16 columns");
         asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, "
@@ -686,7 +690,7 @@ __device__ __forceinline__ void tmem_ld(uint32_t taddr, float (&v)[LW])
                      "tcgen05.wait::ld.sync.aligned;"
                      : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]),
                        "=f"(v[6]), "=f"(v[7])
-                     : "r"(taddr) : "memory");
+                     : "r"(taddr));
     }
 }
 
@@ -743,61 +747,240 @@ __device__ __forceinline__ void copy_data_plane(float *spix, const float *src, i
     cp_async_wait_all();
 }
 
-// Staging of the one-thread-per-ROI kernel (slot g = threadIdx.x holds ROI
-// roi0 + g).  The data plane is copied block-wide; after a barrier each thread
-// finishes its own ROI.  For sCMOS it checks the corners, gathers the ROI's
-// variance tile from the resident map into its tensor-memory lane (pixel p at
-// column p, zeros for an empty or rejected slot), and converts ADU data in
-// place, (ADU - offset) * gain (src/camera_models.jl:110-113); the gathers of
-// 16 pixels are issued before any is used.  The map offset and the ok flag
-// stay in registers, so a ROI takes only its pixels in shared memory.  Every
-// thread of the block calls it (the tensor-memory stores are warp-wide).
-// Returns whether slot g holds a ROI with valid corners.
+// One map column of a ROI, BOX consecutive floats of `map` from a0 + sh with
+// a0 a multiple of 4 (so map + a0 is 16-byte aligned), by aligned float4
+// loads: only the float4s that hold a pixel of the column (each lies inside
+// the map, whose length is a multiple of 4), then the column's floats picked
+// by two levels of selects on the bits of sh (0..3).  With `in` false
+// nothing is loaded and the column is `fill`.
+template <int BOX>
+__device__ __forceinline__ void map_column4(const float *__restrict__ map, long long a0, int sh,
+                                            bool in, float fill, float (&col)[BOX])
+{
+    constexpr int NQ = (BOX + 6) / 4;  // float4s for sh = 3: 4 NQ >= BOX + 3
+    float f[4 * NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+        float4 w = make_float4(fill, fill, fill, fill);
+        if (in && (4 * q < BOX || 4 * q < sh + BOX))
+            w = __ldg(reinterpret_cast<const float4 *>(map + a0) + q);
+        f[4 * q] = w.x;
+        f[4 * q + 1] = w.y;
+        f[4 * q + 2] = w.z;
+        f[4 * q + 3] = w.w;
+    }
+    const bool s0 = sh & 1, s1 = sh & 2;
+    float t[BOX + 2];
+#pragma unroll
+    for (int i = 0; i < BOX + 2; i++) t[i] = s0 ? f[i + 1] : f[i];
+#pragma unroll
+    for (int i = 0; i < BOX; i++) col[i] = s1 ? t[i + 2] : t[i];
+}
+
+// Staging of the one-thread-per-ROI kernel.  Slot g = threadIdx.x of the
+// block holds ROI roi0 + g.  Each lane first checks its own ROI's corners;
+// the map offset and the ok flag stay in its registers, so a ROI takes only
+// its pixels in shared memory.  sCMOS then needs, per ROI, its variance tile
+// in the owning lane's tensor memory (pixel p at column p; zeros for an
+// empty or rejected slot) and, for ADU data, its pixels converted in place,
+// (ADU - offset) * gain (src/camera_models.jl:110-113; rejected ROIs stay as
+// they are).  Two ways are compiled, by box size (each the faster one
+// measured on GB300):
+//
+// * up to 11x11, per lane: the block copies its pixels, and after a barrier
+//   each lane gathers its own ROI's variance, gain and offset.  When the maps
+//   are 16-byte aligned with ny a multiple of 4, every column of a ROI starts
+//   at the same offset (y0 - 1) mod 4 within a float4, so each column is
+//   read by a few aligned float4 loads instead of box scalar loads
+//   (map_column4); otherwise by scalar loads, 16 pixels' worth issued before
+//   any is used.
+// * 13x13 and 15x15, per warp, with no block barrier: warp w stages its own
+//   32 slots.  The variance tiles are copied from the map into the ROIs'
+//   shared-memory slots by 4-byte cp.async, two ROI columns per instruction
+//   (lanes 0-15 column j, 16-31 column j + 1), so consecutive lanes read
+//   consecutive map rows; each lane then moves its slot into its
+//   tensor-memory lane; then the warp's pixels are copied over the slots and
+//   converted with the same coalesced gathers of gain and offset.  The ROI
+//   whose map offset a step needs comes from its lane by a warp shuffle.
+//
+// Every thread of the block calls it (the tensor-memory stores are
+// warp-wide).  Returns whether slot threadIdx.x holds a ROI with valid
+// corners.
 template <int BOX, bool SCMOS>
-__device__ __forceinline__ bool stage_r1(const KernelArgs &a, float *spix, int R, int64_t roi0,
+__device__ __forceinline__ bool stage_r1(const KernelArgs &a, float *spix, int64_t roi0,
                                          int nroi, uint32_t taddr)
 {
     constexpr int B2 = BOX * BOX;
-    copy_data_plane<BOX>(spix, a.data + roi0 * B2, R, nroi);
-    __syncthreads();  // other threads' copies of this thread's ROI
-    const int g = threadIdx.x;
-    bool ok = g < nroi;
-    if (!SCMOS) return ok;
-    long long base = 0;
-    if (ok) {
-        const int32_t x0 = a.xc[roi0 + g], y0 = a.yc[roi0 + g];
-        ok = x0 >= 1 && y0 >= 1 && x0 + BOX - 1 <= a.nx && y0 + BOX - 1 <= a.ny;
-        if (!ok) atomicAdd(a.bad_corners, 1ull);
-        base = ok ? (long long)(y0 - 1) + (long long)a.ny * (long long)(x0 - 1) : 0;
-    }
-    __syncwarp();  // converged for the warp-wide stores
-    float *pix = spix + g * B2;
-    const bool adu = a.adu;  // uniform over the launch
-#pragma unroll
-    for (int c = 0; c < TmemVar<BOX>::CHUNKS; c++) {
-        float v[16], off[16], gn[16];
-#pragma unroll
-        for (int u = 0; u < 16; u++) {
-            const int p = 16 * c + u;
-            const int j = p / BOX, i = p - j * BOX;
-            const long long m = base + i + (long long)a.ny * j;
-            const bool in = ok && p < B2;
-            v[u] = in ? __ldg(a.var + m) : 0.f;
-            off[u] = (adu && in) ? __ldg(a.offset + m) : 0.f;
-            gn[u] = (adu && in) ? __ldg(a.gain + m) : 1.f;
+    if constexpr (!SCMOS || BOX <= 11) {
+        copy_data_plane<BOX>(spix, a.data + roi0 * B2, blockDim.x, nroi);
+        __syncthreads();  // other threads' copies of this thread's ROI
+        const int g = threadIdx.x;
+        bool ok = g < nroi;
+        if (!SCMOS) return ok;
+        long long base = 0;
+        if (ok) {
+            const int32_t x0 = a.xc[roi0 + g], y0 = a.yc[roi0 + g];
+            ok = x0 >= 1 && y0 >= 1 && x0 + BOX - 1 <= a.nx && y0 + BOX - 1 <= a.ny;
+            if (!ok) atomicAdd(a.bad_corners, 1ull);
+            base = ok ? (long long)(y0 - 1) + (long long)a.ny * (long long)(x0 - 1) : 0;
         }
-        tmem_st16(taddr + 16 * c, v);
-        if (adu) {
-            // a rejected or empty slot converts by (x - 0) * 1: unchanged
+        __syncwarp();  // converged for the warp-wide stores
+        float *pix = spix + g * B2;
+        const bool adu = a.adu;  // uniform over the launch
+        // uniform over the launch as well
+        const bool vec = ((reinterpret_cast<uintptr_t>(a.var) | reinterpret_cast<uintptr_t>(a.gain) |
+                           reinterpret_cast<uintptr_t>(a.offset)) & 15u) == 0 && (a.ny & 3) == 0;
+        if (vec) {
+            const int sh = (int)(base & 3);
+            const long long b0 = base - sh;
+            float cb[16];  // the 16-column chunk being assembled for tensor memory
+#pragma unroll
+            for (int j = 0; j < BOX; j++) {
+                const long long aj = b0 + (long long)a.ny * j;
+                float v[BOX];
+                map_column4<BOX>(a.var, aj, sh, ok, 0.f, v);
+                if (adu) {
+                    // a rejected or empty slot converts by (x - 0) * 1: unchanged
+                    float o[BOX], gn[BOX];
+                    map_column4<BOX>(a.offset, aj, sh, ok, 0.f, o);
+                    map_column4<BOX>(a.gain, aj, sh, ok, 1.f, gn);
+#pragma unroll
+                    for (int i = 0; i < BOX; i++)
+                        pix[BOX * j + i] = __fmul_rn(__fadd_rn(pix[BOX * j + i], -o[i]), gn[i]);
+                }
+#pragma unroll
+                for (int i = 0; i < BOX; i++) {
+                    const int p = BOX * j + i;
+                    cb[p & 15] = v[i];
+                    if ((p & 15) == 15) tmem_st16(taddr + (p & ~15), cb);
+                }
+            }
+            if (B2 & 15) {  // the last, partial chunk: zeros past the tile
+#pragma unroll
+                for (int u = B2 & 15; u < 16; u++) cb[u] = 0.f;
+                tmem_st16(taddr + (B2 & ~15), cb);
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < TmemVar<BOX>::CHUNKS; c++) {
+                float v[16], off[16], gn[16];
+#pragma unroll
+                for (int u = 0; u < 16; u++) {
+                    const int p = 16 * c + u;
+                    const int j = p / BOX, i = p - j * BOX;
+                    const long long m = base + i + (long long)a.ny * j;
+                    const bool in = ok && p < B2;
+                    v[u] = in ? __ldg(a.var + m) : 0.f;
+                    off[u] = (adu && in) ? __ldg(a.offset + m) : 0.f;
+                    gn[u] = (adu && in) ? __ldg(a.gain + m) : 1.f;
+                }
+                tmem_st16(taddr + 16 * c, v);
+                if (adu) {
+                    // a rejected or empty slot converts by (x - 0) * 1: unchanged
+#pragma unroll
+                    for (int u = 0; u < 16; u++) {
+                        const int p = 16 * c + u;
+                        if (p < B2) pix[p] = __fmul_rn(__fadd_rn(pix[p], -off[u]), gn[u]);
+                    }
+                }
+            }
+        }
+        tmem_wait_st();
+        return ok;
+    } else {
+        static_assert(BOX <= 16, "two ROI columns per warp instruction");
+        constexpr int NJP = (BOX + 1) / 2;  // column pairs of a ROI
+        const int l = threadIdx.x & 31;
+        const int r0 = threadIdx.x & ~31;  // the warp's first slot
+        const int nw = min(max(nroi - r0, 0), 32);  // ROIs of this warp
+        float *wpix = spix + r0 * B2;
+        const float *src = a.data + (roi0 + r0) * B2;
+        // this lane's place in a column pair: row i of column 2 jp + jj
+        const int i = l & 15, jj = l >> 4;
+        bool ok = l < nw;
+        long long base = 0;
+        if (ok) {
+            const int32_t x0 = a.xc[roi0 + r0 + l], y0 = a.yc[roi0 + r0 + l];
+            ok = x0 >= 1 && y0 >= 1 && x0 + BOX - 1 <= a.nx && y0 + BOX - 1 <= a.ny;
+            if (!ok) atomicAdd(a.bad_corners, 1ull);
+            base = ok ? (long long)(y0 - 1) + (long long)a.ny * (long long)(x0 - 1) : 0;
+        }
+        // variance tiles into the slots (zeros for rejected and empty slots)
+        for (int r = 0; r < 32; r++) {
+            const long long b = __shfl_sync(0xffffffffu, base, r);
+            const bool okr = __shfl_sync(0xffffffffu, ok, r);
+#pragma unroll
+            for (int jp = 0; jp < NJP; jp++) {
+                const int j = 2 * jp + jj;
+                if (i < BOX && j < BOX)
+                    cp_async4(wpix + r * B2 + j * BOX + i,
+                              okr ? a.var + b + i + (long long)a.ny * j : a.var, okr ? 4u : 0u);
+            }
+        }
+        cp_async_wait_all();
+        __syncwarp();
+#pragma unroll
+        for (int c = 0; c < TmemVar<BOX>::CHUNKS; c++) {
+            float v[16];
 #pragma unroll
             for (int u = 0; u < 16; u++) {
                 const int p = 16 * c + u;
-                if (p < B2) pix[p] = __fmul_rn(__fadd_rn(pix[p], -off[u]), gn[u]);
+                v[u] = p < B2 ? wpix[l * B2 + p] : 0.f;
             }
+            tmem_st16(taddr + 16 * c, v);
         }
+        tmem_wait_st();
+        __syncwarp();  // every lane has read its slot
+        // the warp's pixels over the slots
+        const int cnt = nw * B2;
+        if ((reinterpret_cast<uintptr_t>(src) & 15u) == 0) {
+            const int c4 = cnt >> 2;
+            for (int e = l; e < c4; e += 32) cp_async16(wpix + 4 * e, src + 4 * e);
+            for (int e = (c4 << 2) + l; e < cnt; e += 32) cp_async4(wpix + e, src + e, 4);
+        } else {
+            for (int e = l; e < cnt; e += 32) cp_async4(wpix + e, src + e, 4);
+        }
+        for (int e = cnt + l; e < 32 * B2; e += 32) wpix[e] = 0.f;
+        cp_async_wait_all();
+        __syncwarp();
+        // ADU -> e-, two ROIs (2 NJP gathers of each map) in flight at a time
+        if (a.adu) {
+            for (int r = 0; r < nw; r += 2) {
+                float off[2][NJP], gn[2][NJP];
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    // lanes past the warp's ROIs hold ok == false
+                    const long long b = __shfl_sync(0xffffffffu, base, (r + h) & 31);
+                    const bool okr = __shfl_sync(0xffffffffu, ok, (r + h) & 31) && r + h < 32;
+#pragma unroll
+                    for (int jp = 0; jp < NJP; jp++) {
+                        const int j = 2 * jp + jj;
+                        off[h][jp] = 0.f;
+                        gn[h][jp] = 1.f;
+                        if (okr && i < BOX && j < BOX) {
+                            const long long m = b + i + (long long)a.ny * j;
+                            off[h][jp] = __ldg(a.offset + m);
+                            gn[h][jp] = __ldg(a.gain + m);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    if (r + h >= nw) break;
+#pragma unroll
+                    for (int jp = 0; jp < NJP; jp++) {
+                        const int j = 2 * jp + jj;
+                        if (i < BOX && j < BOX) {
+                            float *px = wpix + (r + h) * B2 + j * BOX + i;
+                            *px = __fmul_rn(__fadd_rn(*px, -off[h][jp]), gn[h][jp]);
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+        }
+        return ok;
     }
-    tmem_wait_st();
-    return ok;
 }
 
 // Stage the block's R ROIs (contiguous in global memory) into shared memory
@@ -1087,7 +1270,7 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
 
     const int R = blockDim.x;
     float *spix = smem;
-    const bool valid = stage_r1<BOX, SCMOS>(a, spix, R, roi0, nroi, taddr);
+    const bool valid = stage_r1<BOX, SCMOS>(a, spix, roi0, nroi, taddr);
 
     const int g = threadIdx.x;
     if (__all_sync(0xffffffffu, g >= nroi)) return;
