@@ -56,10 +56,11 @@ TRAFFIC_BYTES_PER_ROI: dict[str, float] = {
     # 90 000 ROIs, 4 threads per ROI, 32 ROIs/block: 150.3 MB read + 5.8 MB written
     "fit_kernel<3, 15, true, false>": 1734.7,
     # 90 000 ROIs, one thread per ROI, 128 ROIs/block (variances in tensor
-    # memory): 148.9 MB read + 5.6 MB written
-    "fit_kernel_r1<3, 15, true, false>": 1716.6,
-    # 240 000 ROIs, one thread per ROI, 64 ROIs/block: 201.7 MB read + 10.5 MB written
-    "fit_kernel_r1<0, 11, true, false>": 884.3,
+    # memory, per-warp staging): 165.0 MB read + 5.4 MB written
+    "fit_kernel_r1<3, 15, true, false>": 1894.0,
+    # 240 000 ROIs, one thread per ROI, 128 ROIs/block (variances in tensor
+    # memory): 194.9 MB read + 8.9 MB written
+    "fit_kernel_r1<0, 11, true, false>": 849.0,
 }
 
 
