@@ -338,7 +338,27 @@ def extras(torch, ctx, dev, steps, peak_inst):
     out["roi-cut-11x11-2e6-from-100-frames-2048x2048"] = {
         "rois_per_s": n / per, "ms_per_launch": per * 1e3, "achieved_gbs": gbs,
         "hbm_frac": gbs / peak, "bytes_per_roi": 2 * box * box * 4 + 12}
-    del frames, rois, fidx, xc, yc
+    # the device ROI generator: 2e6 XYNB 11x11 sCMOS ADU ROIs at random corners
+    from gaussmle_gb300.fitter import make_desc
+    from gaussmle_gb300.models import GaussianXYNB
+    from gaussmle_gb300.constraints import default_constraints
+    g = torch.Generator(device=dev)
+    g.manual_seed(11)
+    u = lambda lo, hi: lo + (hi - lo) * torch.rand(n, generator=g, device=dev)
+    truth = torch.stack([u(4.5, 7.5), u(4.5, 7.5), torch.exp(u(np.log(100.0), np.log(20000.0))),
+                         u(1, 20)], 1).contiguous()
+    psf = GaussianXYNB(1.3)
+    desc = make_desc(psf, box, 20, default_constraints(psf, box), 2)
+    xc = torch.randint(1, 2048 - box + 2, (n,), generator=g, device=dev, dtype=torch.int32)
+    yc = torch.randint(1, 2048 - box + 2, (n,), generator=g, device=dev, dtype=torch.int32)
+    rois = torch.empty(n * box * box, device=dev)
+    dt = time_steps(torch, stream, lambda: G.simulate_rois(ctx, desc, truth, 5, xc, yc, out=rois,
+                                                            stream=stream), steps, 3)
+    per = dt / steps
+    out["roi-generator-11x11-scmos-adu-2e6"] = {
+        "rois_per_s": n / per, "ms_per_launch": per * 1e3,
+        "output_gbs": n * box * box * 4 / per / 1e9}
+    del frames, rois, fidx, xc, yc, truth
     torch.cuda.empty_cache()
     return out
 

@@ -10,11 +10,11 @@ from .constraints import ParameterConstraints, default_constraints
 from .camera import IdealCamera, SCMOSCamera, ROIBatch
 from .fitter import GaussMLEFitter, LocalizationResult, fit, make_desc
 from ._lib import Context, GaussMLEError, FitDesc, load, library_path
-from .device import cut_rois, fit_device
+from .device import cut_rois, fit_device, simulate_rois
 
 __all__ = [
     "GaussianXYNB", "GaussianXYNBS", "GaussianXYNBSXSY", "AstigmaticXYZNB", "PSFModel",
     "model_from_id", "ParameterConstraints", "default_constraints", "IdealCamera",
     "SCMOSCamera", "ROIBatch", "GaussMLEFitter", "LocalizationResult", "fit", "make_desc",
-    "Context", "GaussMLEError", "FitDesc", "load", "library_path", "fit_device", "cut_rois",
+    "Context", "GaussMLEError", "FitDesc", "load", "library_path", "fit_device", "cut_rois", "simulate_rois",
 ]

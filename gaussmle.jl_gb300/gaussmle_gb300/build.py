@@ -26,7 +26,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2",
 SOURCES = [f"gmle_fit_{m}_{cam}.cu" for m in ("astig", "xynbsxsy", "xynbs", "xynb")
            for cam in ("poisson", "scmos")] + ["gmle_runtime.cu", "gmle_server.cu",
                                                 "gmle_noalloc.cu", "gmle_pvalue.cu",
-                                                "gmle_frames.cu"]
+                                                "gmle_frames.cu", "gmle_simulate.cu"]
 
 
 def nvcc() -> str:

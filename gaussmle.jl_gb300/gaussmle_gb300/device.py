@@ -51,3 +51,26 @@ def cut_rois(ctx: _lib.Context, frames, frame_idx, x_corners, y_corners, box: in
                                            ptr(frame_idx), ptr(x_corners), ptr(y_corners), n,
                                            box, ptr(out), C.c_void_p(s.cuda_stream)))
     return out
+
+
+def simulate_rois(ctx: _lib.Context, desc, truth, seed: int, x_corners=None, y_corners=None,
+                  out=None, stream=None):
+    """Synthetic ROIs on the device (gmle_simulate_device).
+
+    `desc` is a fit descriptor (make_desc: model, box, camera, psf in pixel
+    units); `truth` a contiguous (n, P) float32 CUDA tensor of true parameters
+    in the fitted order; sCMOS cameras use the context's calibration maps at
+    the 1-based int32 CUDA corners.  Returns (or fills) the ROI-major stack of
+    n*box*box floats that fit_device takes."""
+    import torch
+    if not (truth.is_cuda and truth.is_contiguous() and truth.dim() == 2):
+        raise ValueError("truth must be a contiguous (n, P) CUDA tensor")
+    n, box = truth.shape[0], desc.box
+    if out is None:
+        out = torch.empty(n * box * box, dtype=torch.float32, device=truth.device)
+    s = stream if stream is not None else torch.cuda.current_stream(truth.device)
+    ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(None)
+    ctx.check(ctx.lib.gmle_simulate_device(ctx.handle, C.byref(desc), ptr(truth), ptr(x_corners),
+                                           ptr(y_corners), n, C.c_uint64(seed), ptr(out),
+                                           C.c_void_p(s.cuda_stream)))
+    return out

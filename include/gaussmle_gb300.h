@@ -191,6 +191,28 @@ gmle_status gmle_cut_rois_device(gmle_ctx *ctx, const float *d_frames, int32_t n
                                  int64_t n, int32_t box, float *d_rois, void *stream);
 
 /*
+ * Synthetic ROIs on the device, in the (box, box, n) layout gmle_fit_device
+ * takes.  Replaces the reference simulator's per-ROI loop
+ * (src/simulator.jl:228-307): pixel (i, j) of ROI k has the expectation
+ * mu = bg + N psf_x(j) psf_y(i) of its true parameters d_truth[P k ...]
+ * ((P, n) column-major, the fitted parameter order of d->model; d->psf as for
+ * fitting; d->iterations and the constraints are not used), then
+ *   GMLE_CAMERA_POISSON:   Poisson(mu);
+ *   GMLE_CAMERA_SCMOS:     Poisson(mu) + Normal(0, variance) in electrons;
+ *   GMLE_CAMERA_SCMOS_ADU: (Poisson(mu) + Normal(0, variance)) / gain + offset,
+ * with the context's calibration maps at the ROI's 1-based corners (row = y;
+ * corners may be NULL for Poisson).  Draws come from a counter-based
+ * Philox4x32-10 stream keyed by `seed`: pixel p of ROI k depends only on
+ * (seed, k, p).  Box sizes 1..32.  An sCMOS ROI whose box lies outside the
+ * maps is filled with NaN and counted by gmle_fit_device_errors.  Device
+ * pointers; enqueued on `stream`.  (No reference counterpart as an API: the
+ * reference generates on the host, with its own random streams.)
+ */
+gmle_status gmle_simulate_device(gmle_ctx *ctx, const gmle_fit_desc *d, const float *d_truth,
+                                 const int32_t *d_x_corners, const int32_t *d_y_corners,
+                                 int64_t n, uint64_t seed, float *d_rois, void *stream);
+
+/*
  * Goodness-of-fit p-values, computed on the GPU.  Replaces the host loop after
  * every fit (src/interface.jl:265-275, :459-468): chi2 = -2 llr in Float32 and
  * p = 1 - Float32(cdf(Chisq(df), chi2)), with df = box^2 - P for a fit of P
