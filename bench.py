@@ -318,6 +318,16 @@ def extras(torch, ctx, dev, steps, peak_inst):
         out[name] = {"fits_per_s": n / per, "ms_per_launch": per * 1e3,
                      "shape": [tpr, rpb], "work_fp32_equiv_per_roi": w["fp32_equiv"],
                      "roofline_frac": n * w["fp32_equiv"] / per / 1e12 / peak_inst}
+        if name == "xynb-11x11-poisson-1e6":
+            # the full-Hessian option (Fisher scoring with LM damping) on the
+            # same ROIs, 20 iterations
+            dlm = make_desc(psf, box, 20, cons, cam, 1)
+            dt = time_steps(torch, stream, lambda: G.fit_device(ctx, dlm, wl["data"], wl["xc"],
+                                                                 wl["yc"], prm, crl, llr, flg,
+                                                                 stream=stream), steps, 3)
+            out["xynb-11x11-poisson-1e6-fisher-lm"] = {
+                "fits_per_s": n * steps / dt, "ms_per_launch": dt / steps * 1e3,
+                "vs_newton": per / (dt / steps)}
         del wl, prm, crl, llr, flg
         torch.cuda.empty_cache()
     # ROI extraction from device-resident frames (gmle_cut_rois_device): an

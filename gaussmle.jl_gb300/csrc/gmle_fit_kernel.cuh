@@ -1211,6 +1211,134 @@ __device__ __forceinline__ void fisher_column(float (&Fh)[P][P], float (&Fl)[P][
         }
 }
 
+// ---- full-Hessian method (GMLE_METHOD_FISHER_LM; no reference counterpart) ----
+//
+// An option beside the reference's per-parameter Newton step: each pass at
+// a candidate theta gives the log-likelihood L (compute_log_likelihood,
+// src/camera_models.jl:60-96), the gradient g_k = sum dudt_k cf (the
+// reference's likelihood terms, src/camera_models.jl:19-42) and the expected
+// information F_kl = sum dudt_k dudt_l / v over mu > 0 (the Fisher matrix of
+// src/unified_kernel.jl:378-396).  A candidate at least as likely as the best
+// so far (to 1e-5 |L|, the rounding of an FP32 sum of up to 225 terms, so that
+// near the maximum the decision does not turn on rounding) is accepted, with
+// its g and F, and the damping lambda falls tenfold; a worse one is rejected
+// and lambda rises tenfold.  The next step
+// solves (F + lambda diag F) step = g at the best point (Fisher scoring with
+// Levenberg-Marquardt damping), clamped like the reference's steps
+// (max_step, then the bounds).  The final pass is the reference's, at the
+// best point.
+
+// Per pixel of a full-Hessian pass: final_pixel's LLR and Fisher weight
+// sums, plus the gradient's row sums R_b += b cf.
+template <bool SCMOS, bool SIG, int NB>
+__device__ __forceinline__ void lm_pixel(float d, float v, float mu, float py, float yd1,
+                                         float ys1, float &llr, float (&Q)[NB][NB],
+                                         float (&Rs)[NB])
+{
+    final_pixel<SCMOS, SIG, NB>(d, v, mu, py, yd1, ys1, llr, Q);
+    float cf, df;
+    likelihood_terms<SCMOS>(d, v, mu, cf, df);
+    Rs[0] = fmaf(py, cf, Rs[0]);
+    Rs[1] = fmaf(yd1, cf, Rs[1]);
+    Rs[2] += cf;
+    if (SIG) Rs[3] = fmaf(ys1, cf, Rs[3]);
+}
+
+// One column's contribution to F (upper triangle) and g, in FP32.
+template <int MODEL, int P, int NB>
+__device__ __forceinline__ void lm_column(float (&F)[P][P], float (&g)[P], const float (&Q)[NB][NB],
+                                          const float (&Rs)[NB], float xp, float xd1, float xs1,
+                                          const AstigWidths &aw)
+{
+    using S = Slots<MODEL>;
+    float av[P][2];
+    av[S::IX][0] = xd1; av[S::IX][1] = 0.f;
+    av[S::IY][0] = xp;  av[S::IY][1] = 0.f;
+    av[S::IN][0] = xp;  av[S::IN][1] = 0.f;
+    av[S::IB][0] = 1.f; av[S::IB][1] = 0.f;
+    if (MODEL == 1) { av[4][0] = xs1; av[4][1] = xp; }
+    if (MODEL == 2) { av[4][0] = xs1; av[4][1] = 0.f; av[5][0] = xp; av[5][1] = 0.f; }
+    if (MODEL == 3) { av[2][0] = xs1 * aw.dsx; av[2][1] = xp * aw.dsy; }
+#pragma unroll
+    for (int k = 0; k < P; k++) {
+#pragma unroll
+        for (int tk = 0; tk < term_count(MODEL, k); tk++)
+            g[k] = fmaf(av[k][tk], Rs[term_b(MODEL, k, tk)], g[k]);
+#pragma unroll
+        for (int l = k; l < P; l++) {
+            float sum = 0.f;
+#pragma unroll
+            for (int tk = 0; tk < term_count(MODEL, k); tk++)
+#pragma unroll
+                for (int tl = 0; tl < term_count(MODEL, l); tl++)
+                    sum = fmaf(av[k][tk] * av[l][tl],
+                               qsym<NB>(Q, term_b(MODEL, k, tk), term_b(MODEL, l, tl)), sum);
+            F[k][l] += sum;
+        }
+    }
+}
+
+// Accept or reject the pass's candidate th (log-likelihood L, gradient g,
+// information F, upper triangle) against the best point thb (Lb, gb, Fb),
+// then the next step from the best point into stp.
+template <int P>
+__device__ __forceinline__ void lm_update(const float (&th)[P], float (&thb)[P], float (&stp)[P],
+                                          float (&gb)[P], float (&Fb)[P][P], float &Lb,
+                                          float &lam, bool first, float L, const float (&g)[P],
+                                          const float (&F)[P][P])
+{
+    if (first || L >= Lb - 1e-5f * fabsf(Lb)) {
+#pragma unroll
+        for (int k = 0; k < P; k++) {
+            thb[k] = th[k];
+            gb[k] = g[k];
+#pragma unroll
+            for (int l = k; l < P; l++) Fb[k][l] = F[k][l];
+        }
+        Lb = L;
+        lam = fmaxf(lam * 0.1f, 1e-7f);
+    } else {
+        lam = fminf(lam * 10.f, 1e7f);
+    }
+    // Cholesky of A = Fb + lam diag(Fb) (lower factor Lm), then two solves
+    float Lm[P][P], y[P];
+    bool ok = true;
+#pragma unroll
+    for (int j = 0; j < P; j++) {
+        float sd = Fb[j][j] + lam * Fb[j][j];
+#pragma unroll
+        for (int k = 0; k < j; k++) sd -= Lm[j][k] * Lm[j][k];
+        ok = ok && sd > 0.f;
+        const float dj = sqrtf(fmaxf(sd, 1e-30f));
+        Lm[j][j] = dj;
+#pragma unroll
+        for (int i = j + 1; i < P; i++) {
+            float si = Fb[j][i];
+#pragma unroll
+            for (int k = 0; k < j; k++) si -= Lm[i][k] * Lm[j][k];
+            Lm[i][j] = __fdiv_rn(si, dj);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < P; i++) {
+        float si = gb[i];
+#pragma unroll
+        for (int k = 0; k < i; k++) si -= Lm[i][k] * y[k];
+        y[i] = __fdiv_rn(si, Lm[i][i]);
+    }
+#pragma unroll
+    for (int i = P - 1; i >= 0; i--) {
+        float si = y[i];
+#pragma unroll
+        for (int k = i + 1; k < P; k++) si -= Lm[k][i] * stp[k];
+        stp[i] = __fdiv_rn(si, Lm[i][i]);
+    }
+    if (!ok) {  // not positive definite: the diagonal step
+#pragma unroll
+        for (int k = 0; k < P; k++) stp[k] = Fb[k][k] > 0.f ? __fdiv_rn(gb[k], Fb[k][k]) : 0.f;
+    }
+}
+
 template <int P>
 __device__ __forceinline__ void write_result(const KernelArgs &a, int64_t roi, bool valid,
                                              const float (&th)[P], double (&Fm)[P][P], float llr)
@@ -1255,7 +1383,7 @@ __device__ __forceinline__ void axis_widths(const float *th, const KernelArgs &a
 // fit_rois_r1 fits ROIs [roi0, roi0 + nroi) of `a` (nroi <= blockDim.x) with
 // the block's threads, staging them in `smem`; the plain kernel calls it once
 // per block, the persistent mixed-batch kernel once per work tile.
-template <int MODEL, int BOX, bool SCMOS>
+template <int MODEL, int BOX, bool SCMOS, bool LM = false>
 __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, int nroi,
                                             float *smem, uint32_t taddr)
 {
@@ -1282,8 +1410,21 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
     initialize<MODEL, BOX, PS>(pix, a.psf, th);
 
     float py[BOX], yd1[BOX], yd2[BOX], ys1[SIG ? BOX : 1], ys2[SIG ? BOX : 1];
+    // full-Hessian method: best point, its log-likelihood, next step, damping
+    constexpr int PL = LM ? P : 1;
+    float thb[PL], stp[PL], gb[PL], Fb[PL][PL], Lb = -INFINITY, lam = 1e-3f;
+#pragma unroll
+    for (int k = 0; k < PL; k++) { thb[k] = th[k]; stp[k] = 0.f; }
     for (int it = 0; it <= a.iterations; ++it) {
         const bool final_pass = (it == a.iterations);
+        if (LM && it > 0) {
+#pragma unroll
+            for (int k = 0; k < PL; k++)
+                th[k] = final_pass ? thb[k]
+                                   : jl_clamp(__fadd_rn(thb[k], jl_clamp(stp[k], -a.max_step[k],
+                                                                         a.max_step[k])),
+                                              a.lower[k], a.upper[k]);
+        }
         float sxw, syw;
         AstigWidths aw;
         axis_widths<MODEL>(th, a, sxw, syw, aw);
@@ -1303,7 +1444,42 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
         float xp, xd1, xd2, xs1 = 0.f, xs2 = 0.f;
         walk_entry<SIG, true>(1, ax, wx, xp, xd1, xd2, xs1, xs2);
 
-        if (!final_pass) {
+        if (LM && !final_pass) {
+            float llr = 0.f;
+            float F[P][P], gs[P];
+#pragma unroll
+            for (int k = 0; k < P; k++) {
+                gs[k] = 0.f;
+#pragma unroll
+                for (int l = 0; l < P; l++) F[k][l] = 0.f;
+            }
+            for (int j = 1; j <= BOX; j++) {
+                float nxp, nxd1, nxd2, nxs1 = 0.f, nxs2 = 0.f;
+                walk_entry<SIG, false>(j + 1, ax, wx, nxp, nxd1, nxd2, nxs1, nxs2);
+                const float npx = N * xp;
+                const float *col = pix + (j - 1) * BOX * PS;
+                float vv[LW];  // this column's variances, from tensor memory
+                if (SCMOS) tmem_ld<LW>(taddr + BOX * (j - 1), vv);
+                float Q[NB][NB], Rs[NB];
+#pragma unroll
+                for (int p = 0; p < NB; p++) {
+                    Rs[p] = 0.f;
+#pragma unroll
+                    for (int q = 0; q < NB; q++) Q[p][q] = 0.f;
+                }
+#pragma unroll
+                for (int t = 0; t < BOX; t++) {
+                    const float d = col[t];
+                    const float v = SCMOS ? vv[t] : 0.f;
+                    const float mu = fmaf(npx, py[t], bg);
+                    lm_pixel<SCMOS, SIG, NB>(d, v, mu, py[t], yd1[t], SIG ? ys1[t] : 0.f, llr, Q,
+                                             Rs);
+                }
+                lm_column<MODEL, P, NB>(F, gs, Q, Rs, xp, xd1, xs1, aw);
+                xp = nxp; xd1 = nxd1; xs1 = nxs1;
+            }
+            if constexpr (LM) lm_update<P>(th, thb, stp, gb, Fb, Lb, lam, it == 0, llr, gs, F);
+        } else if (!final_pass) {
             float py2[BOX], aG[CROSS ? BOX : 1], C[BOX], D[BOX];
 #pragma unroll
             for (int t = 0; t < BOX; t++) {
@@ -1403,7 +1579,7 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
 // sCMOS: warp 0 allocates the CTA's tensor memory for the variance tiles before
 // the first tile and frees it after the last; no path leaves the kernel
 // between the two.
-template <int MODEL, int BOX, bool SCMOS, bool TABLE>
+template <int MODEL, int BOX, bool SCMOS, bool TABLE, bool LM = false>
 __global__ void __launch_bounds__(128) fit_kernel_r1(const KernelArgs a, const TileTable t)
 {
     extern __shared__ __align__(16) float smem[];
@@ -1419,7 +1595,7 @@ __global__ void __launch_bounds__(128) fit_kernel_r1(const KernelArgs a, const T
     if (!TABLE) {
         const int64_t roi0 = (int64_t)blockIdx.x * R;
         const int64_t left = a.n - roi0;
-        fit_rois_r1<MODEL, BOX, SCMOS>(a, roi0, left < R ? (int)left : R, smem, taddr);
+        fit_rois_r1<MODEL, BOX, SCMOS, LM>(a, roi0, left < R ? (int)left : R, smem, taddr);
     } else {
         TableSlot *ts = table_slot(smem, smem_bytes(MODEL, BOX, SCMOS, 1, R));
         table_slot_init(ts);

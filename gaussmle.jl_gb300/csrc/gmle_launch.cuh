@@ -27,11 +27,14 @@ constexpr int kMaxThreadsR1 = 128;
 
 // One launch of a model's kernel.  Plain (t.header == nullptr): ceil(a.n / rpb)
 // blocks over `a`.  Table: `grid` persistent blocks over the table's groups,
-// whose arguments carry this launch's tpr; `a` then only supplies tpr.
+// whose arguments carry this launch's tpr; `a` then only supplies tpr.  `lm`
+// selects the full-Hessian method, which runs in plain one-thread-per-ROI
+// launches only.
 struct LaunchShape {
     int tpr;
     int rois_per_block;
     int64_t grid;  // table launches only
+    bool lm = false;
 };
 
 #define GMLE_DECLARE_FAMILY(M, FAM)                                                           \
@@ -84,27 +87,29 @@ inline size_t launch_smem(int model, int box, bool scmos, int tpr, int rpb, bool
 using FitKernel = void (*)(const KernelArgs, const TileTable);
 
 template <int MODEL, int BOX, bool SCMOS>
-cudaError_t kernel_for(int tpr, bool table, FitKernel *kern)
+cudaError_t kernel_for(int tpr, bool table, bool lm, FitKernel *kern)
 {
     const bool r1 = tpr == 1;
-    *kern = r1 ? (table ? fit_kernel_r1<MODEL, BOX, SCMOS, true> : fit_kernel_r1<MODEL, BOX, SCMOS, false>)
+    if (lm && (!r1 || table)) return cudaErrorInvalidConfiguration;
+    *kern = lm ? fit_kernel_r1<MODEL, BOX, SCMOS, false, true>
+          : r1 ? (table ? fit_kernel_r1<MODEL, BOX, SCMOS, true> : fit_kernel_r1<MODEL, BOX, SCMOS, false>)
                : (table ? fit_kernel<MODEL, BOX, SCMOS, true> : fit_kernel<MODEL, BOX, SCMOS, false>);
     // The largest dynamic shared memory a block may have, once per kernel and
     // device (setting it twice is harmless).
     constexpr int kMaxDevices = 64;
-    static bool done[2][2][kMaxDevices] = {};
+    static bool done[2][2][2][kMaxDevices] = {};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     const bool known = dev >= 0 && dev < kMaxDevices;
-    if (known && done[r1][table][dev]) return cudaSuccess;
+    if (known && done[lm][r1][table][dev]) return cudaSuccess;
     // the 227 KiB a block may use include the kernel's static shared memory
     cudaFuncAttributes fa;
     e = cudaFuncGetAttributes(&fa, *kern);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(*kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              227 * 1024 - (int)fa.sharedSizeBytes);
-    if (e == cudaSuccess && known) done[r1][table][dev] = true;
+    if (e == cudaSuccess && known) done[lm][r1][table][dev] = true;
     return e;
 }
 
@@ -119,7 +124,7 @@ cudaError_t launch_one(const KernelArgs &a, const TileTable &t, const LaunchShap
     if (tpr == 1 && threads > kMaxThreadsR1) return cudaErrorInvalidConfiguration;
     const size_t smem = launch_smem(MODEL, BOX, SCMOS, tpr, rpb, table);
     FitKernel kern;
-    cudaError_t e = kernel_for<MODEL, BOX, SCMOS>(tpr, table, &kern);
+    cudaError_t e = kernel_for<MODEL, BOX, SCMOS>(tpr, table, shape.lm, &kern);
     if (e != cudaSuccess) return e;
     const int64_t blocks = table ? shape.grid : (a.n + rpb - 1) / rpb;
     if (blocks <= 0) return cudaSuccess;
@@ -161,7 +166,7 @@ template <int MODEL, int BOX, bool SCMOS>
 int table_blocks_one(int tpr, int rpb)
 {
     FitKernel kern;
-    cudaError_t e = kernel_for<MODEL, BOX, SCMOS>(tpr, true, &kern);
+    cudaError_t e = kernel_for<MODEL, BOX, SCMOS>(tpr, true, false, &kern);
     if (e != cudaSuccess) return -(int)e;
     const size_t smem = launch_smem(MODEL, BOX, SCMOS, tpr, rpb, true);
     int nb = 0;

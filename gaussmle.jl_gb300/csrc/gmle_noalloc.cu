@@ -100,6 +100,10 @@ gmle_status check_group(const gmle_group &G, int k, bool have_var, bool have_adu
     if (d.iterations < 0) return report(err, err_len, GMLE_INVALID_ARG, "group %d: iterations < 0", k);
     if (d.camera < 0 || d.camera > 2)
         return report(err, err_len, GMLE_INVALID_ARG, "group %d: unknown camera id %d", k, d.camera);
+    if (d.method != GMLE_METHOD_NEWTON)
+        return report(err, err_len, GMLE_INVALID_ARG,
+                      "group %d: method %d runs through gmle_fit and gmle_fit_device only", k,
+                      d.method);
     if (d.model == GMLE_MODEL_XYNB && !(d.psf[0] > 0.f))
         return report(err, err_len, GMLE_INVALID_ARG, "group %d: GaussianXYNB sigma must be > 0", k);
     if (d.model == GMLE_MODEL_ASTIG && (!(d.psf[0] > 0.f) || !(d.psf[1] > 0.f) || d.psf[7] == 0.f))

@@ -61,6 +61,8 @@ gmle_status check_desc(gmle_ctx *ctx, const gmle_fit_desc *d)
     if (d->iterations < 0) return fail(ctx, GMLE_INVALID_ARG, "iterations < 0");
     if (d->camera < 0 || d->camera > 2)
         return fail(ctx, GMLE_INVALID_ARG, "unknown camera id %d", d->camera);
+    if (d->method != GMLE_METHOD_NEWTON && d->method != GMLE_METHOD_FISHER_LM)
+        return fail(ctx, GMLE_INVALID_ARG, "unknown method id %d", d->method);
     if (d->camera != GMLE_CAMERA_POISSON) {
         if (!ctx->d_var) return fail(ctx, GMLE_INVALID_ARG, "sCMOS fit without calibration maps");
         if (d->camera == GMLE_CAMERA_SCMOS_ADU && (!ctx->d_gain || !ctx->d_offset))
@@ -106,8 +108,15 @@ Tuning pick_tuning(gmle_ctx *ctx, const gmle_fit_desc *d, int64_t n)
 {
     const bool scmos = d->camera != GMLE_CAMERA_POISSON;
     auto it = ctx->tuning.find({d->model, d->box, (int)scmos});
-    if (it != ctx->tuning.end()) return it->second;
-    return default_tuning(ctx->num_sms, d->model, d->box, scmos, n);
+    Tuning t = it != ctx->tuning.end() ? it->second
+                                       : default_tuning(ctx->num_sms, d->model, d->box, scmos, n);
+    if (d->method == GMLE_METHOD_FISHER_LM && t.tpr != 1) {
+        // the full-Hessian method runs one thread per ROI; 128-thread blocks
+        // use the tensor memory of sCMOS variance tiles fully
+        t.tpr = 1;
+        t.rois_per_block = scmos ? 128 : 64;
+    }
+    return t;
 }
 
 KernelArgs make_args(gmle_ctx *ctx, const gmle_fit_desc *d, const float *data, const int32_t *xc,
@@ -151,8 +160,9 @@ cudaError_t launch(gmle_ctx *ctx, const gmle_fit_desc *d, const KernelArgs &a, i
 {
     const bool scmos = d->camera != GMLE_CAMERA_POISSON;
     ctx->launches++;
-    return gmle::launch_fit(d->model, d->box, scmos, a, gmle::TileTable{},
-                            gmle::LaunchShape{a.tpr, rpb, 0}, s);
+    gmle::LaunchShape shape{a.tpr, rpb, 0};
+    shape.lm = d->method == GMLE_METHOD_FISHER_LM;
+    return gmle::launch_fit(d->model, d->box, scmos, a, gmle::TileTable{}, shape, s);
 }
 
 bool is_pinned(const void *p)
@@ -531,6 +541,11 @@ gmle_status gmle_autotune(gmle_ctx *ctx, const gmle_fit_desc *desc, const float 
         return fail(ctx, GMLE_INVALID_ARG, "sCMOS fit needs ROI corners");
     cudaSetDevice(ctx->device);
     const bool scmos = desc->camera != GMLE_CAMERA_POISSON;
+    // shapes are kept per (model, box, camera family) and timed with the
+    // reference's method, which runs in every shape
+    gmle_fit_desc dn = *desc;
+    dn.method = GMLE_METHOD_NEWTON;
+    desc = &dn;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0), "cudaEventCreate");
     CK(cudaEventCreate(&e1), "cudaEventCreate");
@@ -634,6 +649,10 @@ gmle_status validate_groups(gmle_ctx *ctx, const gmle_group *groups, int32_t ngr
             return fail(ctx, GMLE_INVALID_ARG, "group %d: sCMOS fit needs ROI corners", k);
         if (G.n > 0x7fffffffLL * 32)
             return fail(ctx, GMLE_INVALID_ARG, "group %d: more ROIs than a table indexes", k);
+        if (G.desc.method != GMLE_METHOD_NEWTON)
+            return fail(ctx, GMLE_INVALID_ARG,
+                        "group %d: method %d runs through gmle_fit and gmle_fit_device only", k,
+                        G.desc.method);
     }
     return GMLE_OK;
 }

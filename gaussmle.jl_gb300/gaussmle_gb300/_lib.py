@@ -45,8 +45,11 @@ class FitDesc(C.Structure):
     _fields_ = [
         ("model", C.c_int32), ("box", C.c_int32), ("iterations", C.c_int32),
         ("camera", C.c_int32), ("psf", C.c_float * 8), ("lower", C.c_float * 6),
-        ("upper", C.c_float * 6), ("max_step", C.c_float * 6),
+        ("upper", C.c_float * 6), ("max_step", C.c_float * 6), ("method", C.c_int32),
     ]
+
+
+METHOD_NEWTON, METHOD_FISHER_LM = 0, 1
 
 
 class Group(C.Structure):

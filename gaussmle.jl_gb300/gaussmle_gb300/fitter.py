@@ -36,12 +36,17 @@ def validate_fit_input(data: np.ndarray) -> None:
 
 
 def make_desc(psf_pixels: PSFModel, box: int, iterations: int,
-              constraints: ParameterConstraints, camera: int) -> _lib.FitDesc:
+              constraints: ParameterConstraints, camera: int,
+              method: int = _lib.METHOD_NEWTON) -> _lib.FitDesc:
+    """gmle_fit_desc.  method: METHOD_NEWTON (the reference's step) or
+    METHOD_FISHER_LM (full-Hessian steps with Levenberg-Marquardt damping, an
+    option with no reference counterpart)."""
     d = _lib.FitDesc()
     d.model = psf_pixels.model_id
     d.box = box
     d.iterations = iterations
     d.camera = camera
+    d.method = method
     P = psf_pixels.nparams
     for t, v in enumerate(psf_pixels.psf_vector()):
         d.psf[t] = float(v)
@@ -56,14 +61,23 @@ def make_desc(psf_pixels: PSFModel, box: int, iterations: int,
 
 class GaussMLEFitter:
     """src/interface.jl:73-145.  `device` must be 'gpu' (or None/'auto'): this
-    library is the GPU device and has no CPU fallback."""
+    library is the GPU device and has no CPU fallback.  `method` is
+    'newton' (the reference's per-parameter Newton step) or 'fisher_lm'
+    (full-Hessian steps with Levenberg-Marquardt damping, an option with no
+    reference counterpart)."""
+
+    METHODS = {"newton": _lib.METHOD_NEWTON, "fisher_lm": _lib.METHOD_FISHER_LM}
 
     def __init__(self, psf_model: PSFModel = GaussianXYNB(0.13), device=None,
                  iterations: int = 20, constraints: ParameterConstraints | None = None,
-                 batch_size: int = 10_000, context: _lib.Context | None = None):
+                 batch_size: int = 10_000, context: _lib.Context | None = None,
+                 method: str = "newton"):
         if device not in (None, "gpu", "auto", ":gpu"):
             raise ValueError(f"device {device!r}: only the GPU device is provided "
                              "(the reference's CPU path is not part of this library)")
+        if method not in self.METHODS:
+            raise ValueError(f"method {method!r}: one of {sorted(self.METHODS)}")
+        self.method = method
         self.psf_model = psf_model
         self.iterations = int(iterations)
         # The reference builds default constraints for an 11x11 box whatever
@@ -135,7 +149,8 @@ def _run(fitter: GaussMLEFitter, data_f: np.ndarray, psf_pixels: PSFModel, camer
     ctx = fitter.context
     box, n = data_f.shape[0], data_f.shape[2]
     P = psf_pixels.nparams
-    desc = make_desc(psf_pixels, box, fitter.iterations, fitter.constraints, camera)
+    desc = make_desc(psf_pixels, box, fitter.iterations, fitter.constraints, camera,
+                     GaussMLEFitter.METHODS[fitter.method])
     params = np.empty((n, P), np.float32)
     crlb = np.empty((n, P), np.float32)
     llr = np.empty(n, np.float32)

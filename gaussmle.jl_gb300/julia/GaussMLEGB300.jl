@@ -32,6 +32,7 @@ struct FitDesc
     lower::NTuple{6,Float32}
     upper::NTuple{6,Float32}
     max_step::NTuple{6,Float32}
+    method::Int32   # 0: the reference's Newton step; 1: full-Hessian (Fisher scoring, LM damping)
 end
 
 model_id(::GaussianXYNB) = Int32(0)
@@ -47,9 +48,9 @@ psf_vector(p::AstigmaticXYZNB) = Float32.((p.σx₀, p.σy₀, p.Ax, p.Ay, p.Bx,
 pad6(v) = ntuple(k -> k <= length(v) ? Float32(v[k]) : 0f0, 6)
 
 function FitDesc(psf_pixels::PSFModel, box::Integer, iterations::Integer, camera::Integer,
-                 c::ParameterConstraints)
+                 c::ParameterConstraints; method::Integer = 0)
     FitDesc(model_id(psf_pixels), Int32(box), Int32(iterations), Int32(camera),
-            psf_vector(psf_pixels), pad6(c.lower), pad6(c.upper), pad6(c.max_step))
+            psf_vector(psf_pixels), pad6(c.lower), pad6(c.upper), pad6(c.max_step), Int32(method))
 end
 
 mutable struct Context

@@ -70,6 +70,18 @@ typedef enum {
                                   applied on the device (src/camera_models.jl:110-113) */
 } gmle_camera;
 
+/* Iteration method of a fit. */
+typedef enum {
+    GMLE_METHOD_NEWTON = 0,    /* the reference's per-parameter Newton step with its diagonal
+                                  Hessian (src/unified_kernel.jl:330-350); the default */
+    GMLE_METHOD_FISHER_LM = 1  /* no reference counterpart: full-Hessian steps, (F + lambda
+                                  diag F) step = gradient with the expected information F
+                                  (Fisher scoring) and Levenberg-Marquardt damping; a step
+                                  that lowers the log-likelihood is rejected (lambda x 10,
+                                  step halved).  Same clamps, same final pass and CRLB.
+                                  gmle_fit and gmle_fit_device only, one thread per ROI */
+} gmle_method;
+
 /* Per-ROI output flag bits */
 #define GMLE_FLAG_CONVERGED 1u /* isfinite(CRLB_x): test/local_performance_benchmark.jl:291-293 */
 #define GMLE_FLAG_CHOLESKY 2u  /* Fisher inverse via Cholesky (src/unified_kernel.jl:412) */
@@ -87,13 +99,14 @@ typedef enum {
  */
 typedef struct {
     int32_t model;      /* gmle_model */
-    int32_t box;        /* ROI edge length, 3..15 (kernels specialised for 7..15) */
+    int32_t box;        /* ROI edge length: 5, 7, 9, 11, 13 or 15 */
     int32_t iterations; /* Newton iterations (reference default 20) */
     int32_t camera;     /* gmle_camera */
     float psf[8];
     float lower[6];
     float upper[6];
     float max_step[6];
+    int32_t method;     /* gmle_method; 0 (zero-initialised) is the reference's */
 } gmle_fit_desc;
 
 typedef struct gmle_ctx gmle_ctx;

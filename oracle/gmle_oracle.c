@@ -54,6 +54,7 @@ typedef struct {
     float lower[6];
     float upper[6];
     float max_step[6];
+    int32_t method;     /* 0 the reference's Newton step, 1 the library's full-Hessian option */
 } oracle_desc;
 
 static inline int oracle_nparams(int model)
@@ -125,6 +126,7 @@ static int check_desc(const oracle_desc *d)
     if (d->box < 3 || d->box > 15) return -2;
     if (d->iterations < 0) return -3;
     if (d->camera < 0 || d->camera > 2) return -4;
+    if (d->method < 0 || d->method > 1) return -5;
     return 0;
 }
 

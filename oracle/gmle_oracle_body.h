@@ -393,7 +393,70 @@ static void FN(fit_one)(const oracle_desc *d, const float *roi_in, int32_t xc, i
     R th[6];
     FN(initialize)(d->model, box, roi, psf, th);
 
-    for (int it = 0; it < d->iterations; it++) {
+    if (d->method == 1) {
+        /* the library's full-Hessian option (no reference counterpart): Fisher
+         * scoring with Levenberg-Marquardt damping.  Each pass at a candidate
+         * gives L, the gradient g_k = sum du_k cf and F_kl = sum du_k du_l / v
+         * (mu > 0).  A candidate at least as likely as the best (to 1e-5 |L|)
+         * is accepted (its g and F kept, lambda / 10); a worse one is rejected
+         * (lambda x 10).  The next step solves (F + lambda diag F) s = g at the best
+         * point by Cholesky (the diagonal step if that fails), clamped like the
+         * reference's steps. */
+        R thb[6], stp[6] = {0}, Lb = (R)-INFINITY, lam = (R)1e-3f, gb[6] = {0}, Fb[36];
+        for (int k = 0; k < P; k++) thb[k] = th[k];
+        for (int t = 0; t < P * P; t++) Fb[t] = 0;
+        for (int it = 0; it < d->iterations; it++) {
+            if (it > 0)
+                for (int k = 0; k < P; k++)
+                    th[k] = FN(jl_clamp)(thb[k] + FN(jl_clamp)(stp[k], -ms[k], ms[k]), lo[k], hi[k]);
+            R L = 0, g[6] = {0}, Fm[36];
+            for (int t = 0; t < P * P; t++) Fm[t] = 0;
+            for (int j = 1; j <= box; j++)
+                for (int i = 1; i <= box; i++) {
+                    int p = (i - 1) + box * (j - 1);
+                    R mu, du[6], d2[6], cf, df;
+                    FN(pixel_derivatives)(d->model, i, j, th, psf, &mu, du, d2);
+                    FN(likelihood_terms)(scmos, roi[p], mu, vroi[p], &cf, &df);
+                    L += FN(log_likelihood_term)(scmos, roi[p], mu, vroi[p]);
+                    for (int k = 0; k < P; k++) g[k] += du[k] * cf;
+                    if (mu > 0) {
+                        R v = scmos ? mu + vroi[p] : mu;
+                        for (int k = 0; k < P; k++)
+                            for (int l = k; l < P; l++) Fm[k + P * l] += du[k] * du[l] / v;
+                    }
+                }
+            if (it == 0 || L >= Lb - (R)1e-5f * FABS(Lb)) {
+                for (int k = 0; k < P; k++) { thb[k] = th[k]; gb[k] = g[k]; }
+                for (int t = 0; t < P * P; t++) Fb[t] = Fm[t];
+                Lb = L;
+                lam = FN(jl_max)(lam * (R)0.1f, (R)1e-7f);
+            } else {
+                lam = FN(jl_min)(lam * (R)10, (R)1e7f);
+            }
+            R A[36], y[6];
+            for (int k = 0; k < P; k++)
+                for (int l = k; l < P; l++) A[l + P * k] = A[k + P * l] = Fb[k + P * l];
+            for (int k = 0; k < P; k++) A[k + P * k] = Fb[k + P * k] + lam * Fb[k + P * k];
+            if (FN(cholesky)(A, P)) {
+                for (int i = 0; i < P; i++) {
+                    R sm = gb[i];
+                    for (int k = 0; k < i; k++) sm -= A[i + P * k] * y[k];
+                    y[i] = sm / A[i + P * i];
+                }
+                for (int i = P - 1; i >= 0; i--) {
+                    R sm = y[i];
+                    for (int k = i + 1; k < P; k++) sm -= A[k + P * i] * stp[k];
+                    stp[i] = sm / A[i + P * i];
+                }
+            } else {
+                for (int k = 0; k < P; k++)
+                    stp[k] = Fb[k + P * k] > 0 ? gb[k] / Fb[k + P * k] : (R)0;
+            }
+        }
+        for (int k = 0; k < P; k++) th[k] = thb[k];
+    }
+
+    for (int it = 0; d->method == 0 && it < d->iterations; it++) {
         R g[6] = {0}, h[6] = {0};
         for (int j = 1; j <= box; j++)
             for (int i = 1; i <= box; i++) {

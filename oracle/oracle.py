@@ -24,7 +24,7 @@ class OracleDesc(C.Structure):
     _fields_ = [
         ("model", C.c_int32), ("box", C.c_int32), ("iterations", C.c_int32),
         ("camera", C.c_int32), ("psf", C.c_float * 8), ("lower", C.c_float * 6),
-        ("upper", C.c_float * 6), ("max_step", C.c_float * 6),
+        ("upper", C.c_float * 6), ("max_step", C.c_float * 6), ("method", C.c_int32),
     ]
 
 
@@ -63,9 +63,11 @@ def nparams(model: int) -> int:
     return 4 if model == 0 else (6 if model == 2 else 5)
 
 
-def make_desc(model, box, iterations, camera, psf, lower, upper, max_step) -> OracleDesc:
+def make_desc(model, box, iterations, camera, psf, lower, upper, max_step,
+              method: int = 0) -> OracleDesc:
     d = OracleDesc()
     d.model, d.box, d.iterations, d.camera = model, box, iterations, camera
+    d.method = method
     for t in range(8):
         d.psf[t] = float(psf[t])
     for k in range(len(lower)):

@@ -45,10 +45,11 @@ def test_abi_version_and_no_device_error(lib):
 
 
 def test_fitdesc_layout_matches_header():
-    # int32 x4 + float x (8 + 6 + 6 + 6)
-    assert C.sizeof(_lib.FitDesc) == 4 * 4 + 4 * 26
+    # int32 x4 + float x (8 + 6 + 6 + 6) + int32 method
+    assert C.sizeof(_lib.FitDesc) == 4 * 4 + 4 * 26 + 4
     assert _lib.FitDesc.psf.offset == 16 and _lib.FitDesc.lower.offset == 48
     assert _lib.FitDesc.upper.offset == 72 and _lib.FitDesc.max_step.offset == 96
+    assert _lib.FitDesc.method.offset == 120
 
 
 def test_fitter_without_gpu_raises():
