@@ -13,13 +13,15 @@
 //   as easy as 1, 2, 3", SC 2011): key = the 64-bit seed, counter = (pixel
 //   index, ROI index low word, high word, block), so a pixel's draws depend
 //   only on (seed, ROI, pixel), whatever the launch shape; a 32-bit word w
-//   gives the uniform (w + 0.5) / 2^32;
-// * Poisson(lam) in double: lam < 10 by inversion (sequential search of the
-//   CDF from exp(-lam)), lam >= 10 by Hormann's transformed rejection with
+//   gives the uniform (w + 0.5) / 2^32 in double, or ((w >> 8) + 0.5) / 2^24
+//   in float (exact in both);
+// * Poisson(lam): lam < 10 by inversion in float (sequential search of the
+//   CDF from expf(-lam)), lam >= 10 by Hormann's transformed rejection with
 //   squeeze (PTRS, "The transformed rejection method for generating Poisson
-//   random variables", 1993); lam <= 0 gives 0 as in the reference;
-// * read noise by Box-Muller from its own counter block;
-// * mu in double from erf-integrated 1-D Gaussians (src/gausslib/
+//   random variables", 1993), in float but for the exact acceptance test at
+//   lam >= 64, in double; lam <= 0 gives 0 as in the reference;
+// * read noise by Box-Muller in float from its own counter block;
+// * mu in float from erf-integrated 1-D Gaussians (src/gausslib/
 //   baselibrary.jl:8-14; astigmatic widths sigma0 sqrt(alpha(z -+ gamma)),
 //   baselibrary.jl:75-83), the camera arithmetic in float in the
 //   reference's order, every operation rounded on its own (no contraction).
@@ -62,72 +64,120 @@ __device__ __forceinline__ Words philox4x32_10(Words c, uint32_t k0, uint32_t k1
 }
 
 __device__ __forceinline__ double to_uniform(uint32_t w) { return ((double)w + 0.5) * 0x1p-32; }
+__device__ __forceinline__ float to_uniform_f(uint32_t w)
+{
+    return ((float)(w >> 8) + 0.5f) * 0x1p-24f;
+}
 
 // The uniforms of one pixel, from blocks 0, 1, 2, ... of its counter.
 struct PixelStream {
     uint32_t k0, k1, p, rlo, rhi, block;
     Words words;
     int used;
-    __device__ double uniform()
+    __device__ uint32_t word()
     {
         if (used == 4) {
             words = philox4x32_10(Words{{p, rlo, rhi, block}}, k0, k1);
             block++;
             used = 0;
         }
-        return to_uniform(words.w[used++]);
+        return words.w[used++];
     }
+    __device__ double uniform() { return to_uniform(word()); }
+    __device__ float uniform_f() { return to_uniform_f(word()); }
 };
+
+// ln k! for integer k >= 0: a table below 10, else the Stirling series
+// (k + 1/2) ln(k + 1) - (k + 1) + ln(2 pi)/2 + 1/(12 (k+1)) - 1/(360 (k+1)^3)
+// for ln Gamma(k + 1), good to 1e-10 there.  Every operation rounded on its
+// own, in float or in double.
+__device__ __forceinline__ double log_factorial_table(int i)
+{
+    return i <= 1 ? 0.0 : i == 2 ? 0.6931471805599453 : i == 3 ? 1.791759469228055
+         : i == 4 ? 3.1780538303479458 : i == 5 ? 4.787491742782046 : i == 6 ? 6.579251212010101
+         : i == 7 ? 8.525161361065415 : i == 8 ? 10.60460290274525 : 12.801827480081469;
+}
+__device__ __forceinline__ float log_factorial_f(float k)
+{
+    if (k < 10.f) return (float)log_factorial_table((int)k);
+    const float x = __fadd_rn(k, 1.0f), rx = __fdiv_rn(1.0f, x);
+    const float corr = __fmul_rn(rx, __fadd_rn(0.0833333333f, -__fmul_rn(__fmul_rn(rx, rx), 0.00277777778f)));
+    return __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(__fadd_rn(k, 0.5f), logf(x)), -x), 0.918938533f), corr);
+}
+__device__ __forceinline__ double log_factorial_d(double k)
+{
+    if (k < 10.0) return log_factorial_table((int)k);
+    const double x = __dadd_rn(k, 1.0), rx = __ddiv_rn(1.0, x);
+    const double corr = __dmul_rn(rx, __dadd_rn(0.083333333333333333,
+                                                -__dmul_rn(__dmul_rn(rx, rx), 0.0027777777777777778)));
+    return __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(__dadd_rn(k, 0.5), log(x)), -x), 0.9189385332046728),
+                     corr);
+}
 
 __device__ int64_t poisson_draw(double lam, PixelStream &s)
 {
     if (!(lam > 0.0)) return 0;
     if (lam < 10.0) {
-        const double u = s.uniform();
-        double p = exp(-lam), f = p;
+        const float lf = (float)lam;
+        const float u = s.uniform_f();
+        float p = expf(-lf), f = p;
         int64_t k = 0;
         while (u > f && k < 1000) {
             k++;
-            p = __dmul_rn(p, __ddiv_rn(lam, (double)k));
-            f = __dadd_rn(f, p);
+            p = __fmul_rn(p, __fdiv_rn(lf, (float)k));
+            f = __fadd_rn(f, p);
         }
         return k;
     }
-    const double slam = sqrt(lam), loglam = log(lam);
-    const double b = __dadd_rn(0.931, __dmul_rn(2.53, slam));
-    const double a = __dadd_rn(-0.059, __dmul_rn(0.02483, b));
-    const double invalpha = __dadd_rn(1.1239, __ddiv_rn(1.1328, __dadd_rn(b, -3.4)));
-    const double vr = __dadd_rn(0.9277, -__ddiv_rn(3.6224, __dadd_rn(b, -2.0)));
+    const float lf = (float)lam;
+    const float slam = __fsqrt_rn(lf);
+    const float b = __fadd_rn(0.931f, __fmul_rn(2.53f, slam));
+    const float a = __fadd_rn(-0.059f, __fmul_rn(0.02483f, b));
+    const float invalpha = __fadd_rn(1.1239f, __fdiv_rn(1.1328f, __fadd_rn(b, -3.4f)));
+    const float vr = __fadd_rn(0.9277f, -__fdiv_rn(3.6224f, __fadd_rn(b, -2.0f)));
+    const double ld = (double)lf, loglam = lf < 64.f ? 0.0 : log(ld);
+    const float loglamf = logf(lf);
     for (int it = 0; it < 10000; it++) {
-        const double u = __dadd_rn(s.uniform(), -0.5);
-        const double v = s.uniform();
-        const double us = __dadd_rn(0.5, -fabs(u));
-        const double k = floor(__dadd_rn(__dadd_rn(__dmul_rn(__dadd_rn(__ddiv_rn(__dmul_rn(2.0, a), us), b), u),
-                                                   lam), 0.43));
-        if (us >= 0.07 && v <= vr) return (int64_t)k;
-        if (k < 0.0 || (us < 0.013 && v > us)) continue;
-        const double lhs = __dadd_rn(__dadd_rn(log(v), log(invalpha)),
-                                     -log(__dadd_rn(__ddiv_rn(a, __dmul_rn(us, us)), b)));
-        const double rhs = __dadd_rn(__dadd_rn(-lam, __dmul_rn(k, loglam)), -lgamma(__dadd_rn(k, 1.0)));
-        if (lhs <= rhs) return (int64_t)k;
+        const float u = __fadd_rn(s.uniform_f(), -0.5f);
+        const float v = s.uniform_f();
+        const float us = __fadd_rn(0.5f, -fabsf(u));
+        const float k = floorf(__fadd_rn(__fadd_rn(__fmul_rn(__fadd_rn(__fdiv_rn(__fmul_rn(2.0f, a), us),
+                                                                       b), u), lf), 0.43f));
+        if (us >= 0.07f && v <= vr) return (int64_t)k;
+        if (k < 0.f || (us < 0.013f && v > us)) continue;
+        // the exact test: log(v invalpha / (a / us^2 + b)) <= log p(k); in
+        // float while its terms stay small, else in double
+        if (lf < 64.f) {
+            const float lhs = __fadd_rn(__fadd_rn(logf(v), logf(invalpha)),
+                                        -logf(__fadd_rn(__fdiv_rn(a, __fmul_rn(us, us)), b)));
+            const float rhs = __fadd_rn(__fadd_rn(-lf, __fmul_rn(k, loglamf)), -log_factorial_f(k));
+            if (lhs <= rhs) return (int64_t)k;
+        } else {
+            const double usd = us, kd = k;
+            const double lhs = __dadd_rn(__dadd_rn(log((double)v), log((double)invalpha)),
+                                         -log(__dadd_rn(__ddiv_rn((double)a, __dmul_rn(usd, usd)),
+                                                        (double)b)));
+            const double rhs = __dadd_rn(__dadd_rn(-ld, __dmul_rn(kd, loglam)), -log_factorial_d(kd));
+            if (lhs <= rhs) return (int64_t)k;
+        }
     }
-    return (int64_t)floor(lam);
+    return (int64_t)floorf(lf);
 }
 
 // erf-integrated 1-D Gaussian of pixel t (1-based) around c with width s.
-__device__ __forceinline__ double integral_1d(int t, double c, double s)
+__device__ __forceinline__ float integral_1d(int t, float c, float s)
 {
-    const double k = __ddiv_rn(1.0, __dmul_rn(1.4142135623730951, s));
-    const double d = __dadd_rn((double)t, -c);
-    return __dmul_rn(0.5, __dadd_rn(erf(__dmul_rn(__dadd_rn(d, 0.5), k)),
-                                    -erf(__dmul_rn(__dadd_rn(d, -0.5), k))));
+    const float k = __fdiv_rn(1.0f, __fmul_rn(1.41421356f, s));
+    const float d = __fadd_rn((float)t, -c);
+    return __fmul_rn(0.5f, __fadd_rn(erff(__fmul_rn(__fadd_rn(d, 0.5f), k)),
+                                     -erff(__fmul_rn(__fadd_rn(d, -0.5f), k))));
 }
 
-__device__ __forceinline__ double astig_width(double s0, double u, double a, double b)
+__device__ __forceinline__ float astig_width(float s0, float u, float a, float b)
 {
-    const double u2 = __dmul_rn(u, u);
-    return __dmul_rn(s0, sqrt(__dadd_rn(__dadd_rn(__dadd_rn(1.0, u2), __dmul_rn(a, __dmul_rn(u2, u))),
-                                        __dmul_rn(b, __dmul_rn(u2, u2)))));
+    const float u2 = __fmul_rn(u, u);
+    return __fmul_rn(s0, __fsqrt_rn(__fadd_rn(__fadd_rn(__fadd_rn(1.0f, u2), __fmul_rn(a, __fmul_rn(u2, u))),
+                                              __fmul_rn(b, __fmul_rn(u2, u2)))));
 }
 
 struct SimArgs {
@@ -145,8 +195,8 @@ struct SimArgs {
 
 __global__ void __launch_bounds__(kSimThreads) simulate_kernel(const SimArgs a, int rois_per_block)
 {
-    __shared__ double s_ax[kSimMaxRois][2][kSimMaxBox];  // [roi][x, y][pixel]
-    __shared__ double s_n[kSimMaxRois], s_bg[kSimMaxRois];
+    __shared__ float s_ax[kSimMaxRois][2][kSimMaxBox];  // [roi][x, y][pixel]
+    __shared__ float s_n[kSimMaxRois], s_bg[kSimMaxRois];
     __shared__ long long s_base[kSimMaxRois];  // map offset of the ROI's first pixel; -1: bad
     const int box = a.box, b2 = box * box;
     const int64_t k0 = (int64_t)blockIdx.x * rois_per_block;
@@ -173,8 +223,8 @@ __global__ void __launch_bounds__(kSimThreads) simulate_kernel(const SimArgs a, 
     for (int e = threadIdx.x; e < nk * 2 * box; e += blockDim.x) {
         const int q = e / (2 * box), r = e - q * 2 * box, ax = r / box, t = r - ax * box;
         const float *th = a.truth + (int64_t)a.P * (k0 + q);
-        const double c = ax == 0 ? th[0] : th[1];
-        double s;
+        const float c = ax == 0 ? th[0] : th[1];
+        float s;
         if (a.model == 0) {
             s = a.psf[0];
         } else if (a.model == 1) {
@@ -182,9 +232,9 @@ __global__ void __launch_bounds__(kSimThreads) simulate_kernel(const SimArgs a, 
         } else if (a.model == 2) {
             s = ax == 0 ? th[4] : th[5];
         } else {
-            const double z = th[2], gam = a.psf[6], d = a.psf[7];
-            s = ax == 0 ? astig_width(a.psf[0], __ddiv_rn(__dadd_rn(z, -gam), d), a.psf[2], a.psf[4])
-                        : astig_width(a.psf[1], __ddiv_rn(__dadd_rn(z, gam), d), a.psf[3], a.psf[5]);
+            const float z = th[2], gam = a.psf[6], d = a.psf[7];
+            s = ax == 0 ? astig_width(a.psf[0], __fdiv_rn(__fadd_rn(z, -gam), d), a.psf[2], a.psf[4])
+                        : astig_width(a.psf[1], __fdiv_rn(__fadd_rn(z, gam), d), a.psf[3], a.psf[5]);
         }
         s_ax[q][ax][t] = integral_1d(t + 1, c, s);
     }
@@ -200,7 +250,7 @@ __global__ void __launch_bounds__(kSimThreads) simulate_kernel(const SimArgs a, 
             continue;
         }
         // mu = bg + N (psf_y[i] psf_x[j])
-        const double mu = __dadd_rn(s_bg[q], __dmul_rn(s_n[q], __dmul_rn(s_ax[q][1][i], s_ax[q][0][j])));
+        const float mu = __fadd_rn(s_bg[q], __fmul_rn(s_n[q], __fmul_rn(s_ax[q][1][i], s_ax[q][0][j])));
         PixelStream st{a.k0, a.k1, (uint32_t)p, (uint32_t)k, (uint32_t)((uint64_t)k >> 32), 0u,
                        Words{}, 4};
         const int64_t cnt = poisson_draw(mu, st);
@@ -211,9 +261,9 @@ __global__ void __launch_bounds__(kSimThreads) simulate_kernel(const SimArgs a, 
         const long long m = base + i + (long long)a.ny * j;
         const Words w = philox4x32_10(Words{{(uint32_t)p, (uint32_t)k, (uint32_t)((uint64_t)k >> 32),
                                              kNoiseBlock}}, a.k0, a.k1);
-        const double u1 = to_uniform(w.w[0]), u2 = to_uniform(w.w[1]);
-        const float z = (float)__dmul_rn(sqrt(__dmul_rn(-2.0, log(u1))),
-                                         cos(__dmul_rn(__dmul_rn(2.0, 3.141592653589793), u2)));
+        const float u1 = to_uniform_f(w.w[0]), u2 = to_uniform_f(w.w[1]);
+        const float z = __fmul_rn(__fsqrt_rn(__fmul_rn(-2.0f, logf(u1))),
+                                  cosf(__fmul_rn(6.28318530717958648f, u2)));
         const float tot = __fadd_rn((float)cnt, __fmul_rn(z, __fsqrt_rn(a.var[m])));
         *dst = a.camera == GMLE_CAMERA_SCMOS ? tot
                                              : __fadd_rn(__fdiv_rn(tot, a.gain[m]), a.offset[m]);

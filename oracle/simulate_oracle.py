@@ -13,17 +13,20 @@ generator defines its own, restated here draw for draw:
 
 * random numbers: Philox4x32-10 (Salmon, Moraes, Dror and Shaw, "Parallel
   random numbers: as easy as 1, 2, 3", SC 2011), key = the 64-bit seed,
-  counter = (pixel index p, ROI index low word, high word, block r); each
-  32-bit word w gives the uniform (w + 0.5) / 2^32 in (0, 1);
-* Poisson(lam): lam < 10 by inversion (sequential search of the CDF from
-  exp(-lam)); lam >= 10 by Hormann's transformed rejection with squeeze
-  (PTRS; W. Hormann, "The transformed rejection method for generating
-  Poisson random variables", Insurance: Mathematics and Economics 12, 1993);
-  both in float64, uniforms taken in order from blocks r = 0, 1, 2, ...;
+  counter = (pixel index p, ROI index low word, high word, block r); a
+  32-bit word w gives the uniform (w + 0.5) / 2^32 in float64 or
+  ((w >> 8) + 0.5) / 2^24 in float32, both exact;
+* Poisson(lam): lam < 10 by inversion in float32 (sequential search of the
+  CDF from exp(-lam)); lam >= 10 by Hormann's transformed rejection with
+  squeeze in float64 (PTRS; W. Hormann, "The transformed rejection method
+  for generating Poisson random variables", Insurance: Mathematics and
+  Economics 12, 1993) in float32, but for the exact acceptance test at
+  lam >= 64, in float64, with ln k! from a table below 10 and the Stirling
+  series above; uniforms taken in order from blocks r = 0, 1, 2, ...;
   lam <= 0 gives 0 as in the reference;
-* read noise: Box-Muller, z = sqrt(-2 ln u1) cos(2 pi u2) from the first
-  two words of block r = 0xFFFF, times sqrt(var);
-* mu in float64 from erf-integrated 1-D Gaussians (src/gausslib/
+* read noise: Box-Muller in float32, z = sqrt(-2 ln u1) cos(2 pi u2) from the
+  first two words of block r = 0xFFFF, times sqrt(var);
+* mu in float32 from erf-integrated 1-D Gaussians (src/gausslib/
   baselibrary.jl:8-14, with the astigmatic widths sigma0 sqrt(alpha(z -+
   gamma)), baselibrary.jl:75-83), then float32 arithmetic for the camera:
   (count + z sqrt(var)) / gain + offset.
@@ -33,7 +36,7 @@ indexes its maps transposed, src/simulator.jl:292-304).
 from __future__ import annotations
 
 import numpy as np
-from scipy.special import erf, gammaln
+from scipy.special import erf
 
 M0, M1 = 0xD2511F53, 0xCD9E8D57
 W0, W1 = 0x9E3779B9, 0xBB67AE85
@@ -68,13 +71,39 @@ class _Stream:
     def block(self, r: int) -> np.ndarray:
         return philox4x32_10(np.array(self.base + [r], np.uint32), self.key)
 
-    def uniform(self) -> float:
+    def word(self) -> int:
         if self.i == 4:
             self.words, self.i = self.block(self.r), 0
             self.r += 1
         w = int(self.words[self.i])
         self.i += 1
-        return (w + 0.5) * 2.0 ** -32
+        return w
+
+    def uniform(self) -> float:
+        return (self.word() + 0.5) * 2.0 ** -32
+
+    def uniform_f(self) -> np.float32:
+        return np.float32((self.word() >> 8) + 0.5) * np.float32(2.0 ** -24)
+
+
+_LOG_FACT = [0.0, 0.0, 0.6931471805599453, 1.791759469228055, 3.1780538303479458,
+             4.787491742782046, 6.579251212010101, 8.525161361065415, 10.60460290274525,
+             12.801827480081469]
+
+
+def log_factorial(k, t):
+    """ln k! in type t (float32 or float64): a table below 10, else the
+    Stirling series (k + 1/2) ln(k + 1) - (k + 1) + ln(2 pi)/2 + 1/(12 (k + 1))
+    - 1/(360 (k + 1)^3)."""
+    if k < 10:
+        return t(_LOG_FACT[int(k)])
+    x = t(k) + t(1.0)
+    rx = t(1.0) / x
+    c = (t(0.0833333333) if t is np.float32 else t(0.083333333333333333),
+         t(0.00277777778) if t is np.float32 else t(0.0027777777777777778),
+         t(0.918938533) if t is np.float32 else t(0.9189385332046728))
+    corr = rx * (c[0] - (rx * rx) * c[1])
+    return (((t(k) + t(0.5)) * np.log(x)) - x + c[2]) + corr
 
 
 def poisson(lam: float, s: _Stream) -> int:
@@ -82,33 +111,45 @@ def poisson(lam: float, s: _Stream) -> int:
     if not lam > 0.0:
         return 0
     if lam < 10.0:
-        u = s.uniform()
-        p = np.exp(-lam)
+        lf = np.float32(lam)
+        u = s.uniform_f()
+        p = np.exp(-lf)
         f = p
         k = 0
         while u > f and k < 1000:
             k += 1
-            p *= lam / k
-            f += p
+            p = np.float32(p * np.float32(lf / np.float32(k)))
+            f = np.float32(f + p)
         return k
-    slam, loglam = np.sqrt(lam), np.log(lam)
-    b = 0.931 + 2.53 * slam
-    a = -0.059 + 0.02483 * b
-    invalpha = 1.1239 + 1.1328 / (b - 3.4)
-    vr = 0.9277 - 3.6224 / (b - 2.0)
+    f32 = np.float32
+    lf = f32(lam)
+    slam = np.sqrt(lf)
+    b = f32(0.931) + f32(2.53) * slam
+    a = f32(-0.059) + f32(0.02483) * b
+    invalpha = f32(1.1239) + f32(1.1328) / (b - f32(3.4))
+    vr = f32(0.9277) - f32(3.6224) / (b - f32(2.0))
+    ld = float(lf)
+    loglam = np.log(ld) if lf >= f32(64.0) else 0.0
+    loglamf = np.log(lf)
     for _ in range(10000):
-        u = s.uniform() - 0.5
-        v = s.uniform()
-        us = 0.5 - abs(u)
-        k = np.floor((2.0 * a / us + b) * u + lam + 0.43)
-        if us >= 0.07 and v <= vr:
+        u = s.uniform_f() - f32(0.5)
+        v = s.uniform_f()
+        us = f32(0.5) - abs(u)
+        k = np.floor(((f32(2.0) * a) / us + b) * u + lf + f32(0.43))
+        if us >= f32(0.07) and v <= vr:
             return int(k)
-        if k < 0.0 or (us < 0.013 and v > us):
+        if k < 0 or (us < f32(0.013) and v > us):
             continue
-        if (np.log(v) + np.log(invalpha) - np.log(a / (us * us) + b)
-                <= -lam + k * loglam - gammaln(k + 1.0)):
+        if lf < f32(64.0):
+            lhs = (np.log(v) + np.log(invalpha)) - np.log(a / (us * us) + b)
+            rhs = (-lf + k * loglamf) - log_factorial(k, f32)
+        else:
+            usd, kd = float(us), float(k)
+            lhs = (np.log(float(v)) + np.log(float(invalpha))) - np.log(float(a) / (usd * usd) + float(b))
+            rhs = (-ld + kd * loglam) - log_factorial(kd, np.float64)
+        if lhs <= rhs:
             return int(k)
-    return int(np.floor(lam))
+    return int(np.floor(np.float32(lam)))
 
 
 def expectation64(model: int, psf, theta: np.ndarray, box: int) -> np.ndarray:
@@ -138,6 +179,36 @@ def expectation64(model: int, psf, theta: np.ndarray, box: int) -> np.ndarray:
     return bg + n * np.outer(axis(y, sy), axis(x, sx))
 
 
+def expectation32(model: int, psf, theta: np.ndarray, box: int) -> np.ndarray:
+    """The generator's (box, box) float32 expectation of one ROI, [row i,
+    column j]: expectation64's formula in float32, each operation rounded."""
+    f = np.float32
+    t = np.asarray(theta, np.float32)
+    psf = np.asarray(psf, np.float32)
+    if model == 3:
+        x, y, z, n, bg = t[:5]
+        sx0, sy0, ax, ay, bx, by, gam, d = psf[:8]
+
+        def width(s0, u, a, b):
+            u2 = u * u
+            return s0 * np.sqrt(((f(1.0) + u2) + a * (u2 * u)) + b * (u2 * u2))
+        sx = width(sx0, (z - gam) / d, ax, bx)
+        sy = width(sy0, (z + gam) / d, ay, by)
+    else:
+        x, y, n, bg = t[:4]
+        sx = sy = psf[0] if model == 0 else t[4]
+        if model == 2:
+            sy = t[5]
+    idx = np.arange(1, box + 1, dtype=np.float32)
+
+    def axis(c, s):
+        k = f(1.0) / (f(1.41421356) * s)
+        lo = erf(((idx - c) - f(0.5)) * k).astype(np.float32)
+        hi = erf(((idx - c) + f(0.5)) * k).astype(np.float32)
+        return (f(0.5) * (hi - lo)).astype(np.float32)
+    return (bg + n * np.outer(axis(y, sy), axis(x, sx)).astype(np.float32)).astype(np.float32)
+
+
 def simulate(model: int, box: int, camera: int, psf, truth: np.ndarray, seed: int,
              maps=None, xc=None, yc=None) -> np.ndarray:
     """(box, box, n) float32 ROIs, as the device generator writes them.
@@ -146,7 +217,7 @@ def simulate(model: int, box: int, camera: int, psf, truth: np.ndarray, seed: in
     n = truth.shape[0]
     out = np.empty((box, box, n), np.float32, order="F")
     for k in range(n):
-        mu = expectation64(model, psf, truth[k], box)
+        mu = expectation32(model, psf, truth[k], box)
         for j in range(box):
             for i in range(box):
                 p = i + box * j
@@ -157,8 +228,10 @@ def simulate(model: int, box: int, camera: int, psf, truth: np.ndarray, seed: in
                     continue
                 var, gain, off = (m[yc[k] - 1 + i, xc[k] - 1 + j] for m in maps)
                 w = s.block(NOISE_BLOCK)
-                u1, u2 = (int(w[0]) + 0.5) * 2.0 ** -32, (int(w[1]) + 0.5) * 2.0 ** -32
-                z = np.float32(np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2))
+                f32 = np.float32
+                u1 = f32((int(w[0]) >> 8) + 0.5) * f32(2.0 ** -24)
+                u2 = f32((int(w[1]) >> 8) + 0.5) * f32(2.0 ** -24)
+                z = np.sqrt(f32(-2.0) * np.log(u1)) * np.cos(f32(6.28318530717958648) * u2)
                 tot = np.float32(cnt) + z * np.sqrt(np.float32(var))
                 out[i, j, k] = tot if camera == 1 else tot / np.float32(gain) + np.float32(off)
     return out
