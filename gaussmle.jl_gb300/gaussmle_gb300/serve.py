@@ -45,7 +45,8 @@ def make_group(psf_pixels: PSFModel, box: int, camera: int, constraints: Paramet
 
 def fit_mixed_device(ctx: _lib.Context, groups: list[_lib.Group], stream=None) -> None:
     """Fit device-resident groups: one persistent table launch per (camera family,
-    model, box) present, plain launches for groups of 65536 ROIs or more."""
+    model, box) present, plain launches for groups of 65536 ROIs or more
+    (gmle_fit_mixed_device; the reference's Newton method only)."""
     import torch
     arr = (_lib.Group * len(groups))(*groups)
     s = stream if stream is not None else torch.cuda.current_stream()
