@@ -177,6 +177,29 @@ def dist_init():
     return world, rank, local
 
 
+def rank_seed(base: int, rank: int) -> int:
+    """Each rank fits its own ROIs (weak scaling: a shard of ROIs per GPU)."""
+    return base + rank
+
+
+def max_over_ranks(x: float, world: int, device="cpu") -> float:
+    """The largest x over the job's ranks (one all-reduce; x itself when
+    world == 1).  device: where the process group's backend reduces (a CUDA
+    device for NCCL, the CPU for gloo)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank: int, steps: int, world: int, seconds_max: float) -> float:
+    """Whole-job throughput: every rank's units over the slowest rank's time."""
+    return units_per_rank * steps * world / seconds_max
+
+
 def set_maps(ctx, maps):
     # (ny, nx) column-major maps are stored as row-major (nx, ny) tensors
     v, g, o = (maps[k].cpu().numpy() for k in ("var", "gain", "offset"))
@@ -386,7 +409,7 @@ def run_ours(args):
     from gaussmle_gb300 import simulate, roofline, serve, loadgen
 
     n = args.n
-    maps, groups = simulate.config3_device(n=n, seed=1003 + rank, device=dev)
+    maps, groups = simulate.config3_device(n=n, seed=rank_seed(1003, rank), device=dev)
     ctx = G.Context(local)
     set_maps(ctx, maps)
     dgs = device_groups(torch, groups, dev)
@@ -422,14 +445,11 @@ def run_ours(args):
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
     clocks = sampler.stop()
-    dt = e0.elapsed_time(e1) / 1e3
+    dt = max_over_ranks(e0.elapsed_time(e1) / 1e3, world, dev)
     if world > 1:
-        t = torch.tensor([dt], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dt = float(t.item())
         dist.barrier()
     launches = ctx.launches() - launches0
-    value = n * args.steps * world / dt
+    value = job_rate(n, args.steps, world, dt)
     per_step = dt / args.steps
     conv = float(np.mean([(b["flags"].cpu().numpy() & 1).mean() for b in dgs]))
 
@@ -474,7 +494,7 @@ def run_ours(args):
     e2e, plain, latency = None, None, None
     if not args.no_e2e or not args.no_latency:
         pools = loadgen.HostPools(groups)
-        reqs = loadgen.make_stream(pools, n, seed=7 + rank)
+        reqs = loadgen.make_stream(pools, n, seed=rank_seed(7, rank))
         srv = serve.Server(ctx, max_inflight_steps=args.max_inflight,
                            use_graphs=bool(args.server_graphs),
                            max_step_rois=args.max_step_rois)
@@ -484,12 +504,14 @@ def run_ours(args):
                     loadgen.run_batch_served(srv, pools, reqs)
                 srv.stats(reset=True)
                 l0 = ctx.launches()
+                if world > 1:
+                    dist.barrier()
                 ts = [loadgen.run_batch_served(srv, pools, reqs) for _ in range(args.steps)]
                 st = srv.stats()
-                et = sum(ts)
+                et = max_over_ranks(sum(ts), world, dev)
                 h2d = sum(r.n * (groups[r.group]["box"] ** 2 * 4 + 8) for r in reqs)
                 d2h = sum(r.n * (2 * groups[r.group]["psf"].nparams * 4 + 5) for r in reqs)
-                e2e = {"value": n * args.steps * world / et, "unit": UNIT,
+                e2e = {"value": job_rate(n, args.steps, world, et), "unit": UNIT,
                        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                        "gpu_launches": ctx.launches() - l0, "ms_per_step": et / args.steps * 1e3,
                        "requests_per_step": len(reqs), "api": "gmle_submit / gmle_wait",
