@@ -60,6 +60,7 @@ inline int kind_of(const gmle_fit_desc &d)
 constexpr size_t kTableHeader = 64;
 struct TableBufs {
     char *h_base = nullptr, *d_base = nullptr;
+    bool in_pool = false;  // h_base points into the set's pool (not freed on its own)
     int64_t cap_groups = 0, cap_tiles = 0;
     unsigned long long *d_counter = nullptr;
     cudaEvent_t reuse = nullptr;  // the last copy reading h_base has completed
@@ -80,6 +81,12 @@ struct MixedSet {
     // serving loop does so: a table copy would queue on the copy engine
     // behind the inputs of every admitted request.
     bool zero_copy = false;
+    // Optional pinned pool (zero-copy sets with one-block-per-tile launches):
+    // each plan carves every kind's table out of it from the start, so a plan
+    // allocates nothing.  The set must not be planned again before its last
+    // plan's launches end.
+    char *pool = nullptr;
+    size_t pool_bytes = 0, pool_used = 0;
     cudaStream_t fork[kForks] = {};
     cudaEvent_t ev_fork = nullptr;
     cudaEvent_t ev_join[kForks] = {};

@@ -616,6 +616,11 @@ void free_table(TableBufs &b)
 gmle_status ensure_table(gmle_ctx *ctx, TableBufs &b, int64_t groups, int64_t tiles,
                          bool device_copy)
 {
+    if (b.in_pool) {  // leaving the pool: a table of its own
+        b.h_base = nullptr;
+        b.cap_groups = b.cap_tiles = 0;
+        b.in_pool = false;
+    }
     if (!b.reuse) {
         CK(cudaEventCreateWithFlags(&b.reuse, cudaEventDisableTiming), "cudaEventCreate");
         CK(cudaEventCreateWithFlags(&b.used, cudaEventDisableTiming), "cudaEventCreate");
@@ -670,7 +675,11 @@ gmle_status init_mixed_set(gmle_ctx *ctx, MixedSet &m)
 
 void free_mixed_set(MixedSet &m)
 {
-    for (TableBufs &b : m.tables) free_table(b);
+    for (TableBufs &b : m.tables) {
+        if (b.in_pool) b.h_base = nullptr;
+        free_table(b);
+    }
+    if (m.pool) cudaFreeHost(m.pool);
     for (int c = 0; c < kForks; c++) {
         if (m.fork[c]) {
             cudaStreamSynchronize(m.fork[c]);
@@ -688,6 +697,7 @@ gmle_status plan_mixed(gmle_ctx *ctx, const gmle_group *groups, int32_t ngroups,
     gmle_status st = validate_groups(ctx, groups, ngroups);
     if (st != GMLE_OK) return st;
     plan = MixedPlan();
+    m.pool_used = 0;
     std::vector<int> by_kind[kKinds];
     int64_t rois[kKinds] = {};
     for (int k = 0; k < ngroups; k++) {
@@ -714,10 +724,23 @@ gmle_status plan_mixed(gmle_ctx *ctx, const gmle_group *groups, int32_t ngroups,
         int64_t tiles = 0;
         for (int k : by_kind[kind]) tiles += (groups[k].n + rpb - 1) / rpb;
         TableBufs &b = m.tables[kind];
-        st = ensure_table(ctx, b, std::max<int64_t>((int64_t)by_kind[kind].size(), opt.reserve_groups),
-                          std::max<int64_t>(tiles, opt.reserve_rois / rpb + opt.reserve_groups),
-                          !m.zero_copy);
-        if (st != GMLE_OK) return st;
+        const int64_t ng = (int64_t)by_kind[kind].size();
+        const size_t need = (kTableHeader + sizeof(KernelArgs) * (size_t)ng + sizeof(int64_t) * (size_t)tiles +
+                             255) & ~size_t(255);
+        if (m.pool && m.zero_copy && !opt.persistent && m.pool_used + need <= m.pool_bytes) {
+            // the kind's table in the set's pool: no allocation
+            if (!b.in_pool && b.h_base) free_table(b);
+            b.h_base = m.pool + m.pool_used;
+            b.in_pool = true;
+            b.cap_groups = ng;
+            b.cap_tiles = tiles;
+            m.pool_used += need;
+        } else {
+            st = ensure_table(ctx, b, std::max<int64_t>(ng, opt.reserve_groups),
+                              std::max<int64_t>(tiles, opt.reserve_rois / rpb + opt.reserve_groups),
+                              !m.zero_copy);
+            if (st != GMLE_OK) return st;
+        }
         if (!m.zero_copy) CK(cudaEventSynchronize(b.reuse), "cudaEventSynchronize");
         int64_t *hdr = reinterpret_cast<int64_t *>(b.h_base);
         KernelArgs *args = reinterpret_cast<KernelArgs *>(b.h_base + kTableHeader);

@@ -45,6 +45,7 @@ constexpr int kMaxSlots = 8;
 // a launch could then wait behind an unrelated one.
 constexpr int kRunStreams = 6;
 constexpr int kServerTableCap = 4096;  // groups (requests) per step and kind
+constexpr size_t kLatencyRecord = 1 << 20;  // latencies kept for the percentiles
 
 enum ReqState { PENDING, STAGED, RUNNING, DRAINING, DONE, FAILED };
 
@@ -217,7 +218,7 @@ struct Server {
         completed++;
         rois_done += r->host.n;
         last_done = r->t_done;
-        if (lat_ms.size() < (1u << 22))
+        if (lat_ms.size() < kLatencyRecord)
             lat_ms.push_back(std::chrono::duration<float, std::milli>(r->t_done - r->t_submit).count());
         cv_done.notify_all();
     }
@@ -517,7 +518,7 @@ gmle_status gmle_server_start(gmle_ctx *ctx, const gmle_server_config *config)
     Server *S = new Server();
     S->ctx = ctx;
     if (config) S->cfg = *config;
-    if (S->cfg.max_inflight_steps <= 0) S->cfg.max_inflight_steps = 8;
+    if (S->cfg.max_inflight_steps <= 0) S->cfg.max_inflight_steps = 4;
     S->cfg.max_inflight_steps = std::min(S->cfg.max_inflight_steps, kMaxSlots);
     if (S->cfg.max_step_rois <= 0) S->cfg.max_step_rois = 1ll << 21;
     if (S->cfg.max_pending <= 0) S->cfg.max_pending = 1 << 16;
@@ -547,12 +548,34 @@ gmle_status gmle_server_start(gmle_ctx *ctx, const gmle_server_config *config)
               cudaStreamCreateWithFlags(&S->s_capture, cudaStreamNonBlocking) == cudaSuccess;
     for (int k = 0; ok && k < kRunStreams; k++)
         ok = cudaStreamCreateWithFlags(&S->s_run[k], cudaStreamNonBlocking) == cudaSuccess;
-    // a slot's tables are pinned host memory read in place by its launches
-    for (int k = 0; k < S->cfg.max_inflight_steps; k++) S->sets[k].zero_copy = true;
+    // a slot's tables are pinned host memory read in place by its launches.
+    // Direct launches take them from one pinned pool per slot, allocated here
+    // for a full step (up to kServerTableCap requests, tiles of >= 16 ROIs), so
+    // that no step allocates: a first allocation would synchronise the device
+    // mid-stream.  Graph replays keep a table per kind at a fixed address.
+    const size_t pool_bytes =
+        ((kTableHeader + 256) * kKinds + sizeof(gmle::KernelArgs) * (size_t)kServerTableCap +
+         sizeof(int64_t) * (size_t)(S->cfg.max_step_rois / 16 + kServerTableCap + kKinds) + 4095) &
+        ~size_t(4095);
+    for (int k = 0; ok && k < S->cfg.max_inflight_steps; k++) {
+        S->sets[k].zero_copy = true;
+        if (!S->cfg.use_graphs) {
+            ok = cudaMallocHost(&S->sets[k].pool, pool_bytes) == cudaSuccess;
+            if (ok) S->sets[k].pool_bytes = pool_bytes;
+        }
+    }
     ctx->server = S;
     if (!ok) {
         server_destroy(ctx);
         return fail(ctx, GMLE_CUDA_ERROR, "cannot create the serving streams and buffers");
+    }
+    // what the loop would otherwise grow while it holds its lock: the latency
+    // record, the ticket table and the request events
+    S->lat_ms.reserve(kLatencyRecord);
+    S->table.reserve(1 << 14);
+    for (int k = 0; k < 512; k++) {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess) S->event_pool.push_back(e);
     }
     S->th = std::thread([S] { S->loop(); });
     return GMLE_OK;

@@ -89,12 +89,20 @@ def make_stream(pools: HostPools, total_rois: int, seed: int = 7, lo: int = 50,
 
 
 def run_batch_served(srv: Server, pools: HostPools, reqs: list[Request]) -> float:
-    """Submit every request at once, wait for all; returns seconds."""
-    t0 = time.perf_counter()
-    tickets = [srv.submit(pools.group_struct(r)) for r in reqs]
-    for t in tickets:
-        srv.wait(t)
-    return time.perf_counter() - t0
+    """Submit every request at once, wait for all; returns seconds (Python's
+    cyclic collector paused meanwhile)."""
+    import gc
+    gc_was = gc.isenabled()
+    gc.disable()
+    try:
+        t0 = time.perf_counter()
+        tickets = [srv.submit(pools.group_struct(r)) for r in reqs]
+        for t in tickets:
+            srv.wait(t)
+        return time.perf_counter() - t0
+    finally:
+        if gc_was:
+            gc.enable()
 
 
 def run_batch_plain(ctx: _lib.Context, pools: HostPools, reqs: list[Request]) -> float:
@@ -116,39 +124,47 @@ def _arrivals(reqs: list[Request], load: float, seed: int) -> np.ndarray:
 
 def run_stream_served(srv: Server, pools: HostPools, reqs: list[Request], load: float,
                       seed: int = 11) -> dict:
-    """Poisson arrivals at `load` ROIs/s into the serving loop."""
+    """Poisson arrivals at `load` ROIs/s into the serving loop.  The client
+    submits from one thread and waits from another, blocking in gmle_wait on
+    the tickets in submission order (no polling of the server's lock);
+    request descriptors are built before the stream starts and Python's
+    cyclic collector is paused during it, so that the client itself does not
+    turn arrivals into bursts."""
+    import gc
+    import queue
     at = _arrivals(reqs, load, seed)
+    structs = [pools.group_struct(r) for r in reqs]
     srv.stats(reset=True)
     lat = []
-    done_lock = threading.Lock()
-    pending: list[tuple[int, float]] = []
-    stop = threading.Event()
+    tickets: queue.SimpleQueue = queue.SimpleQueue()
 
     def waiter():
-        while not stop.is_set() or pending:
-            with done_lock:
-                items = list(pending)
-            for t, ta in items:
-                if srv.poll(t):
-                    lat.append(time.perf_counter() - ta)
-                    with done_lock:
-                        pending.remove((t, ta))
-            time.sleep(0.0002)
+        while True:
+            item = tickets.get()
+            if item is None:
+                return
+            t, ta = item
+            srv.wait(t)
+            lat.append(time.perf_counter() - ta)
 
-    th = threading.Thread(target=waiter)
-    th.start()
-    t0 = time.perf_counter()
-    for r, a in zip(reqs, at):
-        now = time.perf_counter() - t0
-        if now < a:
-            time.sleep(a - now)
-        ta = time.perf_counter()
-        t = srv.submit(pools.group_struct(r))
-        with done_lock:
-            pending.append((t, ta))
-    stop.set()
-    th.join()
-    wall = time.perf_counter() - t0
+    gc_was = gc.isenabled()
+    gc.disable()
+    try:
+        th = threading.Thread(target=waiter)
+        th.start()
+        t0 = time.perf_counter()
+        for g, a in zip(structs, at):
+            now = time.perf_counter() - t0
+            if now < a:
+                time.sleep(a - now)
+            ta = time.perf_counter()
+            tickets.put((srv.submit(g), ta))
+        tickets.put(None)
+        th.join()
+        wall = time.perf_counter() - t0
+    finally:
+        if gc_was:
+            gc.enable()
     st = srv.stats()
     lat_ms = np.array(lat) * 1e3
     # p50/p99: submit -> results on host, timed by the serving loop itself;

@@ -338,7 +338,7 @@ gmle_status gmle_fit_mixed_device_noalloc(const gmle_group *groups, int32_t ngro
  */
 typedef struct {
     int64_t hbm_budget_bytes;   /* device arena; 0 = half of the free HBM at start */
-    int32_t max_inflight_steps; /* concurrent steps; 0 = 8 (at most 8) */
+    int32_t max_inflight_steps; /* concurrent steps; 0 = 4 (at most 8) */
     int64_t max_step_rois;      /* ROIs per step; 0 = 2^21 */
     int32_t max_pending;        /* queued requests before submit rejects; 0 = 1 << 16 */
     int32_t use_graphs;         /* 1: each launch is a replay of a captured CUDA graph of a
