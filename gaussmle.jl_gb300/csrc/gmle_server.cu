@@ -16,6 +16,7 @@
 //              Outputs in pinned (page-locked) host memory are written by the
 //              kernels themselves over the host link, so such a request is
 //              done when its step is: no copy-out call and no output stream.
+//              Pinned corner arrays are likewise read in place.
 // The scheduler never waits on the GPU: it polls events and sleeps briefly when
 // nothing progressed, and no kernel waits on the host.
 #include <cuda_runtime.h>
@@ -59,6 +60,10 @@ struct Request {
     // params, crlb, llr, flags (all pinned, or the request copies them out)
     bool direct_out = false;
     void *out_dev[4] = {};
+    // corners read in place: device addresses of the caller's pinned corners
+    // (sCMOS requests whose both corner arrays are pinned)
+    bool direct_corners = false;
+    const int32_t *corner_dev[2] = {};
     int64_t off = -1, bytes = 0;
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
     Clock::time_point t_submit, t_done;
@@ -166,13 +171,13 @@ struct Server {
         if (e) event_pool.push_back(e);
     }
 
-    static int64_t footprint(const gmle_group &g, bool direct_out)
+    static int64_t footprint(const gmle_group &g, bool direct_out, bool direct_corners)
     {
         const int64_t n = g.n, b2 = (int64_t)g.desc.box * g.desc.box;
         const int P = nparams(g.desc.model);
         int64_t b = align256(4 * n * b2);
         if (!direct_out) b += 2 * align256(4 * n * P) + align256(4 * n) + align256(n);
-        if (g.desc.camera != GMLE_CAMERA_POISSON) b += 2 * align256(4 * n);
+        if (g.desc.camera != GMLE_CAMERA_POISSON && !direct_corners) b += 2 * align256(4 * n);
         return b;
     }
 
@@ -199,7 +204,10 @@ struct Server {
             r->dev.flags = reinterpret_cast<uint8_t *>(p);
             p += align256(n);
         }
-        if (r->host.desc.camera != GMLE_CAMERA_POISSON) {
+        if (r->host.desc.camera != GMLE_CAMERA_POISSON && r->direct_corners) {
+            r->dev.x_corners = r->corner_dev[0];
+            r->dev.y_corners = r->corner_dev[1];
+        } else if (r->host.desc.camera != GMLE_CAMERA_POISSON) {
             r->dev.x_corners = reinterpret_cast<int32_t *>(p);
             p += align256(4 * n);
             r->dev.y_corners = reinterpret_cast<int32_t *>(p);
@@ -239,7 +247,7 @@ struct Server {
         const int64_t n = r->host.n, b2 = (int64_t)r->host.desc.box * r->host.desc.box;
         cudaError_t e = cudaMemcpyAsync((void *)r->dev.data, r->host.data, 4 * n * b2,
                                         cudaMemcpyHostToDevice, s_in);
-        if (e == cudaSuccess && r->host.desc.camera != GMLE_CAMERA_POISSON) {
+        if (e == cudaSuccess && r->host.desc.camera != GMLE_CAMERA_POISSON && !r->direct_corners) {
             e = cudaMemcpyAsync((void *)r->dev.x_corners, r->host.x_corners, 4 * n,
                                 cudaMemcpyHostToDevice, s_in);
             if (e == cudaSuccess)
@@ -620,11 +628,31 @@ gmle_status gmle_submit(gmle_ctx *ctx, const gmle_group *request, uint64_t *tick
             cudaGetLastError();
             r->direct_out = false;
         } else {
-            r->direct_out = at.type == cudaMemoryTypeHost && at.devicePointer != nullptr;
+            // float outputs the kernels write must be 4-byte aligned
+            r->direct_out = at.type == cudaMemoryTypeHost && at.devicePointer != nullptr &&
+                            (k == 3 || (reinterpret_cast<uintptr_t>(outs[k]) & 3) == 0);
             r->out_dev[k] = at.devicePointer;
         }
     }
-    r->bytes = Server::footprint(*request, r->direct_out);
+    // corners in pinned memory are read in place too: one copy per request
+    // (the pixels) instead of three, which matters when many small requests
+    // arrive at once and each copy's fixed cost adds up on the copy engine
+    if (request->desc.camera != GMLE_CAMERA_POISSON && request->x_corners && request->y_corners) {
+        r->direct_corners = true;
+        const int32_t *cs[2] = {request->x_corners, request->y_corners};
+        for (int k = 0; k < 2 && r->direct_corners; k++) {
+            cudaPointerAttributes at;
+            if (cudaPointerGetAttributes(&at, cs[k]) != cudaSuccess) {
+                cudaGetLastError();
+                r->direct_corners = false;
+            } else {
+                r->direct_corners = at.type == cudaMemoryTypeHost && at.devicePointer != nullptr &&
+                                    (reinterpret_cast<uintptr_t>(cs[k]) & 3) == 0;
+                r->corner_dev[k] = static_cast<const int32_t *>(at.devicePointer);
+            }
+        }
+    }
+    r->bytes = Server::footprint(*request, r->direct_out, r->direct_corners);
     r->t_submit = Clock::now();
     {
         std::lock_guard<std::mutex> lk(S->mu);

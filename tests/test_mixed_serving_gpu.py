@@ -222,7 +222,7 @@ def test_many_requests_from_threads(ctx, graphs, pinned):
     (ctypes releases the GIL, so the library sees concurrent calls): each
     slice's results equal those of the same ROIs served as one request.
     Outputs in pageable memory are copied out; outputs in pinned memory are
-    written in place by the kernels."""
+    written in place by the kernels, and pinned corners read in place."""
     import threading
     torch = pytest.importorskip("torch")
 
@@ -255,8 +255,10 @@ def test_many_requests_from_threads(ctx, graphs, pinned):
                 tickets = []
                 for q in part:
                     lo, hi = slices[q]
-                    b = {"data": np.asfortranarray(w.data[:, :, lo:hi]),
-                         "xc": w.x_corners[lo:hi].copy(), "yc": w.y_corners[lo:hi].copy(),
+                    xc, yc = w.x_corners[lo:hi].copy(), w.y_corners[lo:hi].copy()
+                    if pinned:  # corners read in place too
+                        xc, yc = (torch.from_numpy(c).pin_memory().numpy() for c in (xc, yc))
+                    b = {"data": np.asfortranarray(w.data[:, :, lo:hi]), "xc": xc, "yc": yc,
                          "params": out((hi - lo, w.psf.nparams), np.float32, np.nan),
                          "crlb": out((hi - lo, w.psf.nparams), np.float32, np.nan),
                          "llr": out((hi - lo,), np.float32, np.nan),
