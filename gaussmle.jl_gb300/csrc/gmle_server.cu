@@ -551,11 +551,17 @@ gmle_status gmle_server_start(gmle_ctx *ctx, const gmle_server_config *config)
     }
     S->arena.size = budget;
     S->arena.free_[0] = budget;
+    // streams take the device's hardware queues round-robin in creation order
+    // (8 by default): the eight that carry work are created back to back so
+    // that each gets a queue of its own.  An input copy that shared a queue
+    // with a run stream would wait behind the fits launched there.  The capture
+    // stream never submits work, so it comes last and may share a queue.
     bool ok = cudaStreamCreateWithFlags(&S->s_in, cudaStreamNonBlocking) == cudaSuccess &&
-              cudaStreamCreateWithFlags(&S->s_out, cudaStreamNonBlocking) == cudaSuccess &&
-              cudaStreamCreateWithFlags(&S->s_capture, cudaStreamNonBlocking) == cudaSuccess;
+              cudaStreamCreateWithFlags(&S->s_out, cudaStreamNonBlocking) == cudaSuccess;
     for (int k = 0; ok && k < kRunStreams; k++)
         ok = cudaStreamCreateWithFlags(&S->s_run[k], cudaStreamNonBlocking) == cudaSuccess;
+    if (ok && S->cfg.use_graphs)
+        ok = cudaStreamCreateWithFlags(&S->s_capture, cudaStreamNonBlocking) == cudaSuccess;
     // a slot's tables are pinned host memory read in place by its launches.
     // Direct launches take them from one pinned pool per slot, allocated here
     // for a full step (up to kServerTableCap requests, tiles of >= 16 ROIs), so
