@@ -6,7 +6,7 @@ Server: the context's request loop (gmle_server_start / gmle_submit /
 gmle_wait): admission by HBM budget, continuous batching of requests into
 steps of one-block-per-tile table launches (or, with use_graphs, replays of
 CUDA graphs of persistent launches), results written in place into pinned
-host outputs, p50/p99 latency.
+host outputs and pinned corner arrays read in place, p50/p99 latency.
 """
 from __future__ import annotations
 
