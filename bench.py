@@ -254,7 +254,7 @@ def run_reference(args):
     import torch
     from gaussmle_gb300 import simulate
     dev = "cuda:0" if torch.cuda.is_available() else "cpu"
-    maps, groups = simulate.config3_device(n=min(args.n, 200_000), device=dev)
+    maps, groups = simulate.mixed_batch_scmos_device(n=min(args.n, 200_000), device=dev)
     per_step = 20_000
     run, m, nth = oracle_sample(groups, maps, per_step, 0)
     for _ in range(args.warmup):
@@ -409,7 +409,7 @@ def run_ours(args):
     from gaussmle_gb300 import simulate, roofline, serve, loadgen
 
     n = args.n
-    maps, groups = simulate.config3_device(n=n, seed=rank_seed(1003, rank), device=dev)
+    maps, groups = simulate.mixed_batch_scmos_device(n=n, seed=rank_seed(1003, rank), device=dev)
     ctx = G.Context(local)
     set_maps(ctx, maps)
     dgs = device_groups(torch, groups, dev)

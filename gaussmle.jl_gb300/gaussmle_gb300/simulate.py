@@ -143,7 +143,7 @@ def _xy_n_bg(rng, n, box, nlo=500.0, nhi=5000.0, blo=1.0, bhi=20.0, log_n=False)
     return x, y, N, bg
 
 
-def config0(n: int = 10_000, seed: int = 1000) -> Workload:
+def xynb11_poisson(n: int = 10_000, seed: int = 1000) -> Workload:
     rng = np.random.Generator(np.random.Philox(seed))
     box, psf = 11, GaussianXYNB(1.3)
     x, y, N, bg = _xy_n_bg(rng, n, box)
@@ -154,7 +154,7 @@ def config0(n: int = 10_000, seed: int = 1000) -> Workload:
                     data, ones, ones, truth)
 
 
-def config1(n: int = 1_000_000, seed: int = 1001, sensor: int = 2048) -> Workload:
+def xynbs13_scmos(n: int = 1_000_000, seed: int = 1001, sensor: int = 2048) -> Workload:
     rng = np.random.Generator(np.random.Philox(seed))
     box, psf = 13, GaussianXYNBS()
     maps = scmos_maps(rng, sensor, sensor)
@@ -167,7 +167,7 @@ def config1(n: int = 1_000_000, seed: int = 1001, sensor: int = 2048) -> Workloa
                     data, xc, yc, truth, maps=maps)
 
 
-def config2(n: int = 1_000_000, seed: int = 1002) -> Workload:
+def astig15_poisson(n: int = 1_000_000, seed: int = 1002) -> Workload:
     rng = np.random.Generator(np.random.Philox(seed))
     box = 15
     psf = AstigmaticXYZNB(1.3, 1.3, 0.05, 0.05, 0.3, 0.3, 50.0, 100.0)
@@ -210,7 +210,7 @@ def mixed_group(rng, model: int, box: int, n: int, maps, sensor: int) -> Workloa
                     truth, maps=maps)
 
 
-def config3(n: int = 2_000_000, seed: int = 1003, sensor: int = 2048) -> list[Workload]:
+def mixed_batch_scmos(n: int = 2_000_000, seed: int = 1003, sensor: int = 2048) -> list[Workload]:
     rng = np.random.Generator(np.random.Philox(seed))
     maps = scmos_maps(rng, sensor, sensor)
     counts = [int(round(f * n)) for f, _, _ in MIX]
@@ -246,9 +246,10 @@ def _psf_1d_t(torch, centre, sigma, box):
     return 0.5 * (torch.special.erf((t - c + 0.5) / s) - torch.special.erf((t - c - 0.5) / s))
 
 
-def config1_device(n: int = 1_000_000, seed: int = 1001, sensor: int = 2048, device="cuda"):
-    """Workload 1 generated with torch on the device (same distributions as
-    config1(); a different random stream).  Returns a dict of device tensors:
+def xynbs13_scmos_device(n: int = 1_000_000, seed: int = 1001, sensor: int = 2048, device="cuda"):
+    """XYNBS 13x13 sCMOS ADU ROIs at random corners of 2048x2048 maps,
+    generated with torch on the device (the distributions of xynbs13_scmos();
+    a different random stream).  Returns a dict of device tensors:
     data (n*13*13 ROI-major, Julia (box, box, n) layout), xc, yc, var, gain,
     offset ((ny, nx) column-major = tensors of shape (nx, ny)), truth (n, 5)."""
     import torch
@@ -289,7 +290,7 @@ def device_workload(model: int, box: int, camera: int, n: int, seed: int = 2024,
     distributions of the mixed workload (x, y within +-1.5 px of the centre,
     N U(500, 5000), bg U(1, 20); sigma U(1.0, 1.8); sigma_x, sigma_y U(1, 2);
     astigmatic z U(-400, 400) with the (1.3, 1.3, 0.05, 0.05, 0.3, 0.3, 50,
-    100) calibration).  Same return layout as config1_device()."""
+    100) calibration).  Same return layout as xynbs13_scmos_device()."""
     import torch
     g = torch.Generator(device=device)
     g.manual_seed(seed)
@@ -341,8 +342,8 @@ def device_workload(model: int, box: int, camera: int, n: int, seed: int = 2024,
     return out
 
 
-def config3_device(n: int = 2_000_000, seed: int = 1003, sensor: int = 2048, device="cuda"):
-    """Workload 3 on the device: a mixed batch of n ROIs in the MIX proportions
+def mixed_batch_scmos_device(n: int = 2_000_000, seed: int = 1003, sensor: int = 2048, device="cuda"):
+    """The mixed batch on the device: n ROIs in the MIX proportions
     (40% XYNB 11x11, 25% XYNBS 9x9, 15% XYNBSXSY 13x13 with sigma_x, sigma_y
     U(1, 2), 15% astigmatic 15x15, 5% XYNB 7x7), N log-uniform 100..20000,
     bg U(1, 20), sCMOS ADU data on one shared 2048x2048 calibration map set.

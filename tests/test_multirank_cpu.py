@@ -33,7 +33,7 @@ def _rank_main(rank, world, port, q):
         w, r, _ = bench.dist_init()
         dt = bench.max_over_ranks(0.5 + r, w, "cpu")       # ranks took 0.5 s and 1.5 s
         rate = bench.job_rate(1000, 10, w, dt)
-        shard = simulate.config0(n=64, seed=bench.rank_seed(1000, r))
+        shard = simulate.xynb11_poisson(n=64, seed=bench.rank_seed(1000, r))
         q.put((r, w, dt, rate, float(shard.data.sum()), float(shard.truth[:, 0].sum())))
     finally:
         dist.destroy_process_group()
