@@ -3,11 +3,12 @@
 //
 // One scheduler thread per context:
 //   submit  -> pending (FIFO)          gmle_submit, any thread
-//   admit   -> arena allocation (device memory budget), ROIs and corners copied
-//              in on the input stream                        (admission by HBM)
+//   admit   -> arena allocation (device memory budget), ROIs (and corners
+//              not in pinned memory) copied in on the input stream
+//                                                            (admission by HBM)
 //   step    -> every admitted request whose copy has landed joins the next
-//              step: one persistent table launch per (camera family, model,
-//              box) present; up to max_inflight_steps steps run concurrently,
+//              step: one table launch per (camera family, model, box)
+//              present; up to max_inflight_steps steps run concurrently,
 //              their launches spread over a few run streams: one block per
 //              tile, or a replay of a CUDA graph of a persistent launch
 //              captured once per (slot, kind)               (continuous batching)
@@ -16,7 +17,6 @@
 //              Outputs in pinned (page-locked) host memory are written by the
 //              kernels themselves over the host link, so such a request is
 //              done when its step is: no copy-out call and no output stream.
-//              Pinned corner arrays are likewise read in place.
 // The scheduler never waits on the GPU: it polls events and sleeps briefly when
 // nothing progressed, and no kernel waits on the host.
 #include <cuda_runtime.h>
