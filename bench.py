@@ -90,6 +90,12 @@ def parse():
                         "kind, 0 launches one block per tile directly")
     p.add_argument("--load-rois", type=float, default=2e7,
                    help="ROIs of arrivals per load point (bounded to about 1.5 s)")
+    p.add_argument("--plain", default="",
+                   help="MODEL,BOX,CAMERA,N: time only the plain launch of one homogeneous "
+                        "device-resident workload (model 0..3, camera 0..2) and print its line")
+    p.add_argument("--tpr", type=int, default=0,
+                   help="with --plain: threads per ROI (0: the autotuner's choice)")
+    p.add_argument("--rpb", type=int, default=0, help="with --plain: ROIs per block")
     return p.parse_args()
 
 
@@ -167,7 +173,32 @@ def measured_peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
         return json.loads(p.read_text())
-    return {"hbm_gbs": 6800.0, "source": "fallback"}
+    return {"hbm_gbs": 6800.0, "sm_max_mhz": 2070.0, "source": "fallback"}
+
+
+def kernel_roofline(torch, dev, model, box, camera, n, seconds, sgemm_tinst=None) -> dict:
+    """Roofline of one fit launch (gaussmle_gb300.roofline): the bound is the
+    slowest of issue (FP32 + SFU + FP64 lane instructions at 128 per SM per
+    clock), the SFU pipe, the FP64 pipe and HBM, each at its peak.  The issue
+    peak is taken at the GPU's maximum SM clock (MEASURED_PEAKS.json)."""
+    from gaussmle_gb300 import roofline
+    peaks = measured_peaks()
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    mhz = float(peaks.get("sm_max_mhz", 2070.0))
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    r = roofline.roofline(model, box, camera, n, seconds, sms, mhz, hbm)
+    out = {"bound": r["bound"], "achieved": r["achieved_tinst"], "peak": r["peak_tinst"],
+           "unit": "Tinst/s", "frac": r["frac"], "pipe_frac": r["pipe_frac"],
+           "work_per_roi": r["work"], "bytes_per_roi": r["bytes_per_roi"],
+           "hbm": {"achieved_gbs": n * r["bytes_per_roi"] / seconds / 1e9, "peak_gbs": hbm,
+                   "frac": r["pipe_frac"]["hbm"]},
+           "peak_source": (f"issue peak {sms} SMs x 128 lanes x {mhz:.0f} MHz "
+                           f"({'MEASURED_PEAKS.json' if 'source' not in peaks else 'fallback'}"
+                           " sm_max_mhz); HBM: measured copy bandwidth")}
+    if sgemm_tinst is not None:
+        out["sgemm_fp32_tinst"] = sgemm_tinst
+        out["frac_of_sgemm_rate"] = r["achieved_tinst"] / sgemm_tinst
+    return out
 
 
 def dist_init():
@@ -337,10 +368,10 @@ def extras(torch, ctx, dev, steps, peak_inst):
                                                              wl["yc"], prm, crl, llr, flg,
                                                              stream=stream), steps, 3)
         per = dt / steps
-        w = roofline.work_per_roi(model, box, 20, cam)
+        rl = kernel_roofline(torch, dev, model, box, cam, n, per)
         out[name] = {"fits_per_s": n / per, "ms_per_launch": per * 1e3,
-                     "shape": [tpr, rpb], "work_fp32_equiv_per_roi": w["fp32_equiv"],
-                     "roofline_frac": n * w["fp32_equiv"] / per / 1e12 / peak_inst}
+                     "shape": [tpr, rpb], "work_slots_per_roi": rl["work_per_roi"]["slots"],
+                     "roofline_frac": rl["frac"], "bound": rl["bound"]}
         if name == "xynb-11x11-poisson-1e6":
             # the full-Hessian option (Fisher scoring with LM damping) on the
             # same ROIs, 20 iterations
@@ -546,31 +577,22 @@ def run_ours(args):
     k = int(np.argmax(per_group))
     gk = groups[k]
     tpr, rpb = shapes[k]
-    w_roi = roofline.work_per_roi(gk["model"], gk["box"], 20, gk["camera"])["fp32_equiv"]
-    b_roi = roofline.bytes_per_roi(gk["model"], gk["box"], gk["camera"])
     peak_inst = fp32_peak_tinst(torch, dev)
-    achieved = gk["n"] * w_roi / per_group[k] / 1e12
-    peaks = measured_peaks()
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    hbm_ach = gk["n"] * b_roi / per_group[k] / 1e9
     kname = (f"{'fit_kernel_r1' if tpr == 1 else 'fit_kernel'}<{gk['model']}, {gk['box']}, "
              f"{str(gk['camera'] != 0).lower()}, false>")
     traffic = TRAFFIC_BYTES_PER_ROI.get(kname)
-    rl = {
-        "bound": "fp32+sfu", "achieved": achieved, "peak": peak_inst, "unit": "Tinst/s",
-        "frac": achieved / peak_inst,
+    rl = kernel_roofline(torch, dev, gk["model"], gk["box"], gk["camera"], gk["n"],
+                         per_group[k], peak_inst)
+    rl.update({
         "traffic": traffic * gk["n"] if traffic is not None else None,
         "kernel": f"{kname} (tpr {tpr}, {rpb} ROIs/block), {gk['n']} ROIs per launch",
         "ms_per_launch": per_group[k] * 1e3,
-        "work_per_roi_fp32_equiv": w_roi,
-        "peak_source": "measured in this run: FP32 SGEMM 8192^3 (TF32 off), FFMA lane rate",
-        "hbm": {"achieved_gbs": hbm_ach, "peak_gbs": hbm_peak, "frac": hbm_ach / hbm_peak,
-                "bytes_per_roi": b_roi,
-                "peak_source": "MEASURED_PEAKS.json" if "source" not in peaks else "fallback"},
         "launches": [{"model": g["psf"].__class__.__name__, "box": g["box"], "n": g["n"],
-                      "shape": list(sh), "ms": t * 1e3}
+                      "shape": list(sh), "ms": t * 1e3,
+                      "frac": kernel_roofline(torch, dev, g["model"], g["box"], g["camera"],
+                                              g["n"], t)["frac"]}
                      for g, sh, t in zip(groups, shapes, per_group)],
-    }
+    })
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         cpu = cpu_baseline(groups, maps, args.cpu_seconds)
@@ -602,10 +624,51 @@ def run_ours(args):
     print(json.dumps(out))
 
 
+def run_plain(args):
+    """One homogeneous device-resident workload, plain launches only."""
+    import torch
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    import gaussmle_gb300 as G
+    from gaussmle_gb300 import simulate, tuning
+    from gaussmle_gb300.fitter import make_desc
+    model, box, cam, n = (int(float(x)) for x in args.plain.split(","))
+    ctx = G.Context(0)
+    wl = simulate.device_workload(model, box, cam, n, device=dev)
+    if cam:
+        set_maps(ctx, wl)
+    psf, P = wl["psf"], wl["psf"].nparams
+    cons = simulate.ASTIG_WIDE if model == 3 else G.default_constraints(psf, 11)
+    desc = make_desc(psf, box, 20, cons, cam)
+    prm = torch.empty((n, P), device=dev)
+    crl = torch.empty((n, P), device=dev)
+    llr = torch.empty(n, device=dev)
+    flg = torch.empty(n, dtype=torch.uint8, device=dev)
+    if args.tpr:
+        ctx.check(ctx.lib.gmle_set_tuning(ctx.handle, model, box, cam, args.tpr, args.rpb))
+        tpr, rpb = args.tpr, args.rpb
+    else:
+        tpr, rpb, _ = tuning.autotune(ctx, desc, wl["data"], wl["xc"], wl["yc"], prm, crl, llr,
+                                      flg, save=False)
+    stream = torch.cuda.Stream(dev)
+    l0 = ctx.launches()
+    dt = time_steps(torch, stream, lambda: G.fit_device(ctx, desc, wl["data"], wl["xc"],
+                                                         wl["yc"], prm, crl, llr, flg,
+                                                         stream=stream), args.steps,
+                    args.warmup)
+    per = dt / args.steps
+    rl = kernel_roofline(torch, dev, model, box, cam, n, per)
+    print(json.dumps({"workload": f"plain model {model} box {box} camera {cam} n {n}",
+                      "fits_per_s": n / per, "ms_per_launch": per * 1e3, "shape": [tpr, rpb],
+                      "launches": ctx.launches() - l0, "roofline": rl}))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.plain:
+        run_plain(args)
     else:
         run_ours(args)
 

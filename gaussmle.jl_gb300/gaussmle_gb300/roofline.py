@@ -1,11 +1,20 @@
 """Work and traffic per ROI: the one definition the benchmark's roofline uses.
 
-The fit has no dense contraction, so the bound is the slower of
-  (a) bytes in and out over HBM bandwidth, and
-  (b) the per-ROI FP32 + SFU (MUFU) + FP64 instruction count at peak,
-with SFU and FP64 instructions converted into FP32 issue slots by the lane
-ratios of a GB300 SM (MUFU 16 : FP32 128 lanes per clock -> 8 slots; FP64
-about 2 : 128 -> 64 slots), i.e. as if the pipes did not overlap.
+The fit has no dense contraction, so no tensor-core peak applies.  Its bound
+is the slowest of the resources one ROI uses, each at its peak:
+  * HBM:  algorithmic bytes in and out / HBM bandwidth;
+  * issue: every FP32, SFU (MUFU) and FP64 lane instruction takes an issue
+    slot, and an SM issues at most 128 lane instructions per clock (4
+    schedulers x 32 lanes), which is also the FP32 pipe's rate;
+  * SFU:  16 MUFU lanes per SM per clock, i.e. a MUFU instruction holds its
+    pipe for 8 FP32 issue slots;
+  * FP64: about 2 lanes per SM per clock on GB300 (1/64 of FP32).
+The pipes run concurrently, so the instruction bound of a ROI is
+  max(fp32 + sfu + fp64,  8 sfu,  64 fp64)   FP32 lane-instruction slots
+(``work_per_roi()["slots"]``), and the roofline time of n ROIs is
+  max(n bytes / HBM, n slots / issue peak).
+``fp32_equiv_sum`` = fp32 + 8 sfu + 64 fp64 treats the pipes as if they never
+overlapped; it is kept only as a labelled pessimistic variant.
 
 Counts follow the minimum of the algorithm the kernel implements, which is
 already far below the reference's per-pixel recomputation
@@ -21,12 +30,14 @@ Instruction cost table (lane instructions):
   erf 1 SFU + 10 FP32;  exp, log 1 SFU + 2 FP32;  reciprocal 1 SFU + 1 FP32;
   IEEE division 1 SFU + 7 FP32;  sqrt 1 SFU + 1 FP32;
   add / mul / fma / min / compare / select: 1 FP32.
-Loads, stores, integer and control instructions are not counted.
+Loads, stores, integer and control instructions are not counted: they are
+the kernel's overhead, which the measured instruction count per ROI shows.
 """
 from __future__ import annotations
 
 SFU_SLOTS = 8.0     # FP32 lanes per MUFU lane in one SM (128 / 16)
 FP64_SLOTS = 64.0   # FP32 / FP64 throughput on GB300
+LANES_PER_SM = 128  # FP32 lane instructions issued per SM per clock
 
 NPARAMS = {0: 4, 1: 5, 2: 6, 3: 5}
 
@@ -39,7 +50,11 @@ def _c(erf=0, exp=0, log=0, rcp=0, div=0, sqrt=0, fp32=0):
 
 
 def work_per_roi(model: int, box: int, iterations: int = 20, camera: int = 0) -> dict:
-    """Lane-instruction counts of one ROI fit (see the module docstring)."""
+    """Lane-instruction counts of one ROI fit (see the module docstring).
+
+    Returns fp32, sfu, fp64 (lane instructions), issue (= their sum), slots
+    (the overlapping-pipe bound in FP32 lane slots, the roofline's work) and
+    fp32_equiv_sum (the non-overlapping variant)."""
     P = NPARAMS[model]
     sig = model != 0
     scmos = camera != 0
@@ -76,9 +91,10 @@ def work_per_roi(model: int, box: int, iterations: int = 20, camera: int = 0) ->
     init = 3 * box * box + 40
     fp32 = iterations * it[0] + fin[0] + init
     sfu = iterations * it[1] + fin[1]
-    return {"fp32": fp32, "sfu": sfu, "fp64": fp64,
-            "fp32_equiv": fp32 + SFU_SLOTS * sfu + FP64_SLOTS * fp64,
-            "issue": fp32 + sfu + fp64}
+    issue = fp32 + sfu + fp64
+    return {"fp32": fp32, "sfu": sfu, "fp64": fp64, "issue": issue,
+            "slots": max(issue, SFU_SLOTS * sfu, FP64_SLOTS * fp64),
+            "fp32_equiv_sum": fp32 + SFU_SLOTS * sfu + FP64_SLOTS * fp64}
 
 
 def bytes_per_roi(model: int, box: int, camera: int = 0, flags: bool = True) -> int:
@@ -93,3 +109,28 @@ def bytes_per_roi(model: int, box: int, camera: int = 0, flags: bool = True) -> 
         inp += 12 * b2
     out = 8 * P + 4 + (1 if flags else 0)
     return inp + out
+
+
+def issue_peak_tinst(sm_count: int, sm_mhz: float) -> float:
+    """FP32 issue peak of the GPU [T lane instructions/s]: 128 per SM per clock."""
+    return sm_count * LANES_PER_SM * sm_mhz * 1e6 / 1e12
+
+
+def roofline(model: int, box: int, camera: int, n: int, seconds: float, sm_count: int,
+             sm_mhz: float, hbm_gbs: float, iterations: int = 20) -> dict:
+    """Roofline of one launch of n ROIs that took `seconds`: each resource's
+    time at its peak, the bound (the largest), and the launch's fraction of it
+    (bound time / measured time)."""
+    w = work_per_roi(model, box, iterations, camera)
+    b = bytes_per_roi(model, box, camera)
+    peak = issue_peak_tinst(sm_count, sm_mhz)             # T FP32 lane slots/s
+    t_issue = n * w["issue"] / (peak * 1e12)
+    t_sfu = n * w["sfu"] * SFU_SLOTS / (peak * 1e12)
+    t_fp64 = n * w["fp64"] * FP64_SLOTS / (peak * 1e12)
+    t_hbm = n * b / (hbm_gbs * 1e9)
+    terms = {"issue": t_issue, "sfu": t_sfu, "fp64": t_fp64, "hbm": t_hbm}
+    bound = max(terms, key=terms.get)
+    return {"bound": bound, "frac": terms[bound] / seconds,
+            "achieved_tinst": n * w["slots"] / seconds / 1e12, "peak_tinst": peak,
+            "pipe_frac": {k: v / seconds for k, v in terms.items()},
+            "work": w, "bytes_per_roi": b}
