@@ -242,7 +242,8 @@ def set_maps(ctx, maps):
 # ---------------------------------------------------------------------------
 
 def oracle_sample(groups, maps, m_total: int, threads: int):
-    """Time the FP32 CPU restatement on a proportional sample of the batch."""
+    """Time the FP32 CPU restatement on a proportional sample of the batch:
+    the first m_g ROIs of each group.  run() returns the oracle's outputs."""
     sys.path.insert(0, str(ROOT))
     from oracle import oracle as O
     var, gain, off = (maps[k].cpu().numpy().T for k in ("var", "gain", "offset"))
@@ -258,24 +259,60 @@ def oracle_sample(groups, maps, m_total: int, threads: int):
         jobs.append((d, data, g["xc"][:m].cpu().numpy(), g["yc"][:m].cpu().numpy(), m))
 
     def run():
-        t = time.perf_counter()
-        for d, data, xc, yc, m in jobs:
-            O.fit(d, data, xc, yc, (var, gain, off), "f32", threads)
-        return time.perf_counter() - t
+        return [O.fit(d, data, xc, yc, (var, gain, off), "f32", threads)
+                for d, data, xc, yc, m in jobs]
 
+    run.jobs = jobs
+    run.maps = (var, gain, off)
     return run, sum(j[4] for j in jobs), O.max_threads()
 
 
-def cpu_baseline(groups, maps, seconds: float) -> dict:
+def parity_report(run, outs, gpu_out, groups, n_fp64: int = 3000) -> dict:
+    """Parity of the GPU's outputs for the oracle sample's ROIs (the same
+    ROIs of the timed batch) against the FP32 oracle, and of both against the
+    FP64 oracle on the first n_fp64 ROIs of each group plus every ROI that
+    misses the bar (at most 2000 of them per group)."""
+    from oracle import oracle as O
+    from oracle import parity
+    rep = {"bar": "pos/sigma/z 1e-3, N/bg 1e-4 rel, CRLB 1e-3 rel, same flag",
+           "reference_bar": "test/gpu_tests.jl:224-226", "groups": []}
+    tot = ok = 0
+    for (d, data, xc, yc, m), f32, g, go in zip(run.jobs, outs, groups, gpu_out):
+        gpu = {k: go[k][:m] for k in ("params", "crlb", "llr", "flags")}
+        okm, _ = parity.compare(g["model"], gpu["params"], gpu["crlb"], gpu["flags"], f32)
+        miss = np.nonzero(~okm)[0][:2000]
+        sel = np.unique(np.concatenate([np.arange(min(m, n_fp64)), miss]))
+        sub = data[:, :, sel]
+        f64 = O.fit(d, sub, xc[sel], yc[sel], run.maps, "f64")
+        gf = O.final_at(d, sub, gpu["params"][sel], xc[sel], yc[sel], run.maps, "f64")
+        ff = O.final_at(d, sub, f32["params"][sel], xc[sel], yc[sel], run.maps, "f64")
+        st = parity.group_report(g["model"], gpu, f32, f64, sel, gf, ff)
+        st.update({"model": g["psf"].__class__.__name__, "box": g["box"]})
+        rep["groups"].append(st)
+        tot += st["n"]
+        ok += st["n"] - st["misses"]
+    rep["rois"] = tot
+    rep["pass_frac"] = ok / max(tot, 1)
+    return rep
+
+
+def cpu_baseline(groups, maps, seconds: float, gpu_out=None) -> dict:
     run, m, nth = oracle_sample(groups, maps, 4000, 0)
-    t0 = run()
+    t0 = time.perf_counter()
+    run()
+    t0 = time.perf_counter() - t0
     scale = max(1.0, seconds / max(t0, 1e-6))
     run, m, nth = oracle_sample(groups, maps, int(4000 * scale), 0)
-    t = run()
-    return {"value": m / t, "unit": UNIT, "cores": nth, "kind": "port",
-            "sample": f"{m} ROIs of the mixed batch, in its proportions ({t:.1f} s on {nth} "
-                      "host threads; FP32 restatement of the reference CPU path, "
-                      "oracle/gmle_oracle.c)"}
+    t = time.perf_counter()
+    outs = run()
+    t = time.perf_counter() - t
+    out = {"value": m / t, "unit": UNIT, "cores": nth, "kind": "port",
+           "sample": f"{m} ROIs of the mixed batch, in its proportions (the first ROIs of each "
+                     f"group; {t:.1f} s on {nth} host threads; FP32 restatement of the "
+                     "reference CPU path, oracle/gmle_oracle.c)"}
+    if gpu_out is not None:
+        out["parity"] = parity_report(run, outs, gpu_out, groups)
+    return out
 
 
 def run_reference(args):
@@ -481,6 +518,9 @@ def run_ours(args):
         dist.barrier()
     launches = ctx.launches() - launches0
     value = job_rate(n, args.steps, world, dt)
+    # the timed step's outputs (host copies, outside the timed region), for
+    # the parity check of the oracle sample's ROIs
+    gpu_out = [{k: b[k].cpu().numpy() for k in ("params", "crlb", "llr", "flags")} for b in dgs]
     per_step = dt / args.steps
     conv = float(np.mean([(b["flags"].cpu().numpy() & 1).mean() for b in dgs]))
 
@@ -595,7 +635,7 @@ def run_ours(args):
     })
     cpu = None
     if not args.no_cpu_baseline and world == 1:
-        cpu = cpu_baseline(groups, maps, args.cpu_seconds)
+        cpu = cpu_baseline(groups, maps, args.cpu_seconds, gpu_out)
     ext = None
     if not args.no_extras and world == 1:
         del dgs

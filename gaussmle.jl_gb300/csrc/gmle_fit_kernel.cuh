@@ -11,14 +11,15 @@
 //    the Julia (box, box, n) layout; it stages them into shared memory with
 //    coalesced 16-byte loads (plus the sCMOS variance tile gathered from the
 //    resident calibration map, with the ADU->e- conversion fused in).
-//  * `tpr` lanes (1..32, a power of two) fit one ROI; lane r owns a
-//    contiguous block of pixel columns.  Per Newton iteration the model is
+//  * `tpr` lanes (1, 2, 4 or 8) fit one ROI; with several, each lane owns a
+//    block of pixel columns and rows.  Per Newton iteration the model is
 //    separable: per axis the erf/exp terms are evaluated once per pixel edge
-//    (box + 1 per axis instead of 4 per pixel), the y-axis tables are shared
-//    through shared memory and held in registers, and per pixel only the
-//    likelihood terms are formed and summed into per-column and per-row sums.
-//  * Gradient and diagonal Hessian are summed with warp shuffles; every lane
-//    of the group then applies the same Newton step, so theta stays identical.
+//    (box + 1 per axis instead of 4 per pixel) into tables held in registers,
+//    and per pixel only the likelihood terms are formed and summed into
+//    per-column and per-row sums.
+//  * With several lanes, the gradient and diagonal Hessian are summed with
+//    warp shuffles; every lane of the group then applies the same Newton
+//    step, so theta stays identical.
 //  * Final pass: FP32 per-pixel Fisher products, summed per column in FP32
 //    (<= 15 terms) and across columns and lanes as a compensated double-float
 //    (FP64-class accuracy at FP32 cost); Cholesky (LU fallback) inversion in
@@ -28,6 +29,8 @@
 #include <cuda_runtime.h>
 #include <limits.h>
 #include <stdint.h>
+
+#include <type_traits>
 
 namespace gmle {
 
@@ -78,8 +81,6 @@ template <> struct ModelInfo<1> { static constexpr int P = 5; static constexpr b
 template <> struct ModelInfo<2> { static constexpr int P = 6; static constexpr bool SIG = true; };
 template <> struct ModelInfo<3> { static constexpr int P = 5; static constexpr bool SIG = true; };
 
-// Number of per-axis tables: psf, D1 (d/dpos), D2 (d2/dpos2) [, S1 (d/dsigma), S2].
-template <int MODEL> __host__ __device__ constexpr int ntables() { return ModelInfo<MODEL>::SIG ? 5 : 3; }
 
 constexpr uint8_t FLAG_CONVERGED = 1, FLAG_CHOLESKY = 2, FLAG_LU = 4, FLAG_SINGULAR = 8;
 
@@ -111,6 +112,53 @@ __device__ __forceinline__ float jl_pow4f(float x)
 __device__ __forceinline__ float jl_pow5f(float x)
 {
     return __fmul_rn(x, jl_pow4f(x));
+}
+
+// ---- fast elementary functions -----------------------------------------------
+//
+// The library's erff costs 28 issued instructions, expf 9 and __fdividef(1, x)
+// 4 on GB300; the fit evaluates them per pixel edge and per pixel.  These
+// replacements use single SFU instructions (PTX rcp.approx / ex2.approx,
+// flush-to-zero: subnormal results are 0) and, for erf, the exponential that
+// the fit already evaluates at the same pixel edge.
+
+// 1/x, within 1 ulp
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+// 2^x, within 2 ulp
+__device__ __forceinline__ float ex2_approx(float x)
+{
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+// exp(-t^2 / 2) = 2^(t^2 * (-log2(e) / 2)); the rounding of the exponent
+// costs at most |t^2| 2^-23 relative, i.e. nothing where the value matters.
+__device__ __forceinline__ float gauss_edge(float t)
+{
+    return ex2_approx(__fmul_rn(t, t) * -0.72134752044448170368f);
+}
+// erf(x), given e = exp(-x^2) (the caller's gauss_edge at the same edge).
+// Hastings' form (Abramowitz & Stegun 7.1.26): erf(|x|) = 1 - e t P(t) with
+// t = 1 / (1 + p |x|), here with P of degree 5 refitted by a least-squares
+// (Lawson) minimax fit of exp(-x^2) erfcx(x) on [0, 6]: p = 0.39, 8.3e-9 largest
+// error in exact arithmetic, below 4e-7 absolute evaluated in FP32 (most of it
+// near x = 0, from 1 - e t P(t)); erf(-x) = -erf(x).  Checked against the
+// library's erff by tests/test_math_gpu.py.
+__device__ __forceinline__ float erf_from_gauss(float x, float e)
+{
+    const float t = rcp_approx(fmaf(0.39f, fabsf(x), 1.0f));
+    float p = -0.22753699123859406f;
+    p = fmaf(p, t, 0.8866637945175171f);
+    p = fmaf(p, t, -0.6353994011878967f);
+    p = fmaf(p, t, 0.6495586633682251f);
+    p = fmaf(p, t, 0.09138870239257812f);
+    p = fmaf(p, t, 0.2353251725435257f);
+    return copysignf(fmaf(-e, t * p, 1.0f), x);
 }
 
 // ---- per-axis coefficients (hoisted out of the pixel loops) ----------------
@@ -161,6 +209,7 @@ __device__ __forceinline__ Axis make_axis(float c, float s, float N, float sqrt2
 struct EdgeWalk {
     float ua;    // erf-argument offset (t - c) + 1/2 of the previous pixel's upper edge
     float erfa;  // erf(ua * sq)
+    float ea;    // exp-argument offset (t + 1/2) - c of the previous pixel's upper edge
     float fa;    // exp at the previous pixel's upper edge
 };
 
@@ -169,11 +218,12 @@ __device__ __forceinline__ EdgeWalk walk_start(int t0, const Axis &a)
 {
     const float tf = (float)t0;
     const float ub = __fadd_rn(tf - a.c, -0.5f);
-    const float tb = (__fadd_rn(tf, -0.5f) - a.c) * a.inv_s;
+    const float eb = __fadd_rn(tf, -0.5f) - a.c;
     EdgeWalk w;
     w.ua = ub;
-    w.erfa = erff(__fmul_rn(ub, a.sq));
-    w.fa = expf(-0.5f * __fmul_rn(tb, tb));
+    w.ea = eb;
+    w.fa = gauss_edge(eb * a.inv_s);
+    w.erfa = erf_from_gauss(__fmul_rn(ub, a.sq), w.fa);
     return w;
 }
 
@@ -190,14 +240,17 @@ __device__ __forceinline__ void walk_entry(int t, const Axis &a, EdgeWalk &w, fl
     const float tf = (float)t;
     const float tc = tf - a.c;
     const float ua = __fadd_rn(tc, 0.5f), ub = __fadd_rn(tc, -0.5f);
-    float erfb = w.erfa;
-    if (ub != w.ua) erfb = erff(__fmul_rn(ub, a.sq));
-    const float erfa = erff(__fmul_rn(ua, a.sq));
-    psf = 0.5f * (erfa - erfb);
-    const float ea = __fadd_rn(tf, 0.5f) - a.c, eb = __fadd_rn(tf, -0.5f) - a.c;
+    // the lower edge's exp argument (t - 1/2) - c is the previous upper edge's
+    // ((t - 1) + 1/2) - c: the same two operands, the same float
+    const float ea = __fadd_rn(tf, 0.5f) - a.c, eb = w.ea;
     const float fb = w.fa;
-    const float ta = ea * a.inv_s;
-    const float fa = expf(-0.5f * __fmul_rn(ta, ta));
+    const float fa = gauss_edge(ea * a.inv_s);
+    float erfb = w.erfa;
+    if (ub != w.ua) erfb = erf_from_gauss(__fmul_rn(ub, a.sq), fb);
+    const float erfa = erf_from_gauss(__fmul_rn(ua, a.sq), fa);
+    // the true value is >= 0 (erf is increasing and ua > ub), so is the
+    // reference's; a negative rounding residue of the tails is cut to 0
+    psf = fmaxf(0.5f * (erfa - erfb), 0.0f);
     d1 = a.cst * (fa - fb);
     if (SECOND) d2 = a.cst2 * (ea * fa - eb * fb);
     if (SIG) {
@@ -206,6 +259,7 @@ __device__ __forceinline__ void walk_entry(int t, const Axis &a, EdgeWalk &w, fl
     }
     w.ua = ua;
     w.erfa = erfa;
+    w.ea = ea;
     w.fa = fa;
 }
 
@@ -311,11 +365,11 @@ __device__ __forceinline__ double dd_to_double(float hi, float lo)
 // ---- initialisation, src/unified_kernel.jl:158-255 (one lane, reference order,
 // no FMA contraction so that the start point matches the FP32 reference) ----
 
-template <int MODEL, int BOX, int STRIDE>
-__device__ void initialize(const float *roi_pix, const float *psf, float *th)
+// roi(p) gives pixel p = (i - 1) + BOX (j - 1) of the ROI; BOX may be a
+// compile-time constant (the specialised kernels) or the run-time box.
+template <int MODEL, typename Roi>
+__device__ __forceinline__ void initialize_box(const int BOX, Roi roi, const float *psf, float *th)
 {
-    // roi_pix holds the ROI's pixels STRIDE floats apart (2: (data, variance) pairs)
-    auto roi = [&](int p) { return roi_pix[STRIDE * p]; };
     float edge_sum = 0.f;
     int edge_count = 0;
     for (int j = 1; j <= BOX; j++)
@@ -363,6 +417,13 @@ __device__ void initialize(const float *roi_pix, const float *psf, float *th)
         }
         th[0] = x; th[1] = y; th[2] = z; th[3] = photons; th[4] = bg;
     }
+}
+
+template <int MODEL, int BOX, int STRIDE>
+__device__ void initialize(const float *roi_pix, const float *psf, float *th)
+{
+    // roi_pix holds the ROI's pixels STRIDE floats apart (2: (data, variance) pairs)
+    initialize_box<MODEL>(BOX, [&](int p) { return roi_pix[STRIDE * p]; }, psf, th);
 }
 
 // ---- FP64 CRLB from the Fisher matrix, src/unified_kernel.jl:399-431 --------
@@ -494,8 +555,7 @@ __device__ uint8_t crlb_from_fisher(double (&F)[P][P], float *crlb)
 
 // Shared memory, as arrays over the R ROI slots of a block: pixels (float, or
 // float2 (data in e-, read-noise variance) for sCMOS), for sCMOS the map
-// offset of each ROI's first pixel (int64), one ok flag per slot, and, when
-// several lanes share a ROI (tpr > 1), NT * BOX y-axis table entries.
+// offset of each ROI's first pixel (int64), and one ok flag per slot.
 //
 // One thread per ROI (tpr == 1) keeps only the data plane in shared memory:
 // with sCMOS data each thread's variance tile lives in its tensor-memory lane
@@ -503,10 +563,9 @@ __device__ uint8_t crlb_from_fisher(double (&F)[P][P], float *crlb)
 // (stage_r1), so a ROI takes box^2 floats.
 __host__ __device__ inline size_t smem_bytes(int model, int box, bool scmos, int tpr, int rois)
 {
+    (void)model;
     if (tpr == 1) return (size_t)rois * sizeof(float) * box * box;
-    const int nt = model == 0 ? 3 : 5;
-    return (size_t)rois * (sizeof(float) * ((size_t)box * box * (scmos ? 2 : 1) +
-                                            (size_t)nt * box) +
+    return (size_t)rois * (sizeof(float) * (size_t)box * box * (scmos ? 2 : 1) +
                            (scmos ? sizeof(long long) : 0) + sizeof(int));
 }
 
@@ -628,9 +687,10 @@ template <int BOX> struct TmemVar {
 
 __host__ __device__ constexpr int tmem_var_cols(int box)
 {
-    return box == 5 ? TmemVar<5>::NCOLS : box == 7 ? TmemVar<7>::NCOLS
-         : box == 9 ? TmemVar<9>::NCOLS : box == 11 ? TmemVar<11>::NCOLS
-         : box == 13 ? TmemVar<13>::NCOLS : TmemVar<15>::NCOLS;
+    // TmemVar<box>::NCOLS for a run-time box
+    const int b2 = box * box, lw = box <= 8 ? 8 : 16, chunks = (b2 + 15) / 16;
+    const int need = chunks * 16 > box * (box - 1) + lw ? chunks * 16 : box * (box - 1) + lw;
+    return need <= 32 ? 32 : need <= 64 ? 64 : need <= 128 ? 128 : need <= 256 ? 256 : 512;
 }
 
 template <int NCOLS>
@@ -1073,21 +1133,41 @@ template <int MODEL> struct Slots {
 };
 
 // Likelihood terms of one pixel: compute_likelihood_terms, Poisson
-// src/camera_models.jl:19-34 and sCMOS :36-42 (1/x by __fdividef, 2 ulp).
+// src/camera_models.jl:19-34 and sCMOS :36-42 (1/x by rcp_approx, 1 ulp).
 template <bool SCMOS>
 __device__ __forceinline__ void likelihood_terms(float d, float v, float mu, float &cf, float &df)
 {
     if (!SCMOS) {
-        const float rm = __fdividef(1.0f, mu);
+        const float rm = rcp_approx(mu);
         const float q = d * rm;
         const bool pos = mu > 0.01f;
         cf = pos ? fminf(q - 1.0f, 1e4f) : 0.f;
         df = pos ? fminf(q * rm, 1e4f) : 0.f;
     } else {
-        const float rv = __fdividef(1.0f, mu + v);
+        const float rv = rcp_approx(mu + v);
         cf = (d - mu) * rv;
         df = rv;
     }
+}
+
+// Poisson terms where neither the mu > 0.01 test nor the 1e4 caps can act
+// (uncapped() below): the same values without the tests.
+__device__ __forceinline__ void likelihood_terms_uncapped(float d, float mu, float &cf, float &df)
+{
+    const float rm = rcp_approx(mu);
+    const float q = d * rm;
+    cf = q - 1.0f;
+    df = q * rm;
+}
+
+// Whether a Poisson fit's pixel terms need no mu > 0.01 test and no 1e4 cap
+// in this iteration: mu = fma(N psf_x, psf_y, bg) >= bg > 0.01 when N >= 0
+// (psf >= 0 by construction), and with dmax the ROI's largest pixel,
+// d / mu - 1 < d / bg <= 9900 and d / mu^2 <= d / bg^2 <= 9900 stay below the
+// caps with room for the reciprocal's rounding.  NaN fails every test.
+__device__ __forceinline__ bool uncapped(float N, float bg, float dmax)
+{
+    return bg > 0.01f && N >= 0.f && dmax <= 9900.f * fminf(bg, bg * bg);
 }
 
 // Column-side contributions to gradient gs and diagonal Hessian hs of one pixel
@@ -1186,6 +1266,7 @@ template <bool SCMOS, bool SIG, int NB>
 __device__ __forceinline__ void final_pixel(float d, float v, float mu, float py, float yd1,
                                             float ys1, float &llr, float (&Q)[NB][NB])
 {
+    const float rv = rcp_approx(SCMOS ? mu + v : mu);
     if (!SCMOS) {
         if (mu > 0.f && d > 0.f)
             llr += d * logf(mu) - mu - (d * logf(d) - d);
@@ -1195,10 +1276,10 @@ __device__ __forceinline__ void final_pixel(float d, float v, float mu, float py
         const float tv = mu + v;
         if (tv > 0.f) {
             const float res = d - mu;
-            llr += -0.5f * __fdiv_rn(res * res, tv);
+            llr += -0.5f * ((res * res) * rv);
         }
     }
-    const float w = mu > 0.f ? __fdividef(1.0f, SCMOS ? mu + v : mu) : 0.f;
+    const float w = mu > 0.f ? rv : 0.f;
     const float t0 = py * w, t1 = yd1 * w;
     Q[0][0] = fmaf(t0, py, Q[0][0]);
     Q[0][1] = fmaf(t0, yd1, Q[0][1]);
@@ -1444,6 +1525,15 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
 #pragma unroll
     for (int k = 0; k < P; k++) th[k] = 0.f;
     initialize<MODEL, BOX, PS>(pix, a.psf, th);
+    // Poisson: the ROI's largest pixel (NaN if any pixel is NaN), for uncapped()
+    float dmax = 0.f;
+    if (!SCMOS && !LM) {
+        dmax = -INFINITY;
+        for (int p = 0; p < B2; p++) {
+            const float d = pix[p];
+            dmax = (d > dmax || d != d) ? d : dmax;
+        }
+    }
 
     float py[BOX], yd1[BOX], yd2[BOX], ys1[SIG ? BOX : 1], ys2[SIG ? BOX : 1];
     // full-Hessian method: best point, its log-likelihood, next step, damping
@@ -1537,43 +1627,58 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
             constexpr bool PIPE = SCMOS && BOX >= 15;
             float vv[LW];
             if (PIPE) tmem_ld<LW>(taddr, vv);
-            for (int j = 1; j <= BOX; j++) {
-                // next column's table entry: independent of this column's pixels
-                float nxp, nxd1, nxd2, nxs1 = 0.f, nxs2 = 0.f;
-                walk_entry<SIG, true>(j + 1, ax, wx, nxp, nxd1, nxd2, nxs1, nxs2);
-                const float npx = N * xp, xp2 = xp * xp;
-                const float *col = pix + (j - 1) * BOX * PS;
-                float nv[LW];
-                if (PIPE && j < BOX) tmem_ld_start<LW>(taddr + BOX * j, nv);
-                if (SCMOS && !PIPE) tmem_ld<LW>(taddr + BOX * (j - 1), vv);
-                // even and odd rows in separate partial sums: two independent
-                // FMA chains of box/2 instead of one of box
-                float A[2] = {0.f, 0.f}, B[2] = {0.f, 0.f}, E[2] = {0.f, 0.f},
-                      F[2] = {0.f, 0.f}, Gc[2] = {0.f, 0.f};
+            // the column loop, with (UNCAPPED) or without the Poisson terms'
+            // tests and caps
+            auto columns = [&](auto uncapped_tag) {
+                constexpr bool UNCAPPED = decltype(uncapped_tag)::value;
+                for (int j = 1; j <= BOX; j++) {
+                    // next column's table entry: independent of this column's pixels
+                    float nxp, nxd1, nxd2, nxs1 = 0.f, nxs2 = 0.f;
+                    walk_entry<SIG, true>(j + 1, ax, wx, nxp, nxd1, nxd2, nxs1, nxs2);
+                    const float npx = N * xp, xp2 = xp * xp;
+                    const float *col = pix + (j - 1) * BOX * PS;
+                    float nv[LW];
+                    if (PIPE && j < BOX) tmem_ld_start<LW>(taddr + BOX * j, nv);
+                    if (SCMOS && !PIPE) tmem_ld<LW>(taddr + BOX * (j - 1), vv);
+                    // even and odd rows in separate partial sums: two independent
+                    // FMA chains of box/2 instead of one of box
+                    float A[2] = {0.f, 0.f}, B[2] = {0.f, 0.f}, E[2] = {0.f, 0.f},
+                          F[2] = {0.f, 0.f}, Gc[2] = {0.f, 0.f};
 #pragma unroll
-                for (int t = 0; t < BOX; t++) {
-                    const float d = col[t];
-                    const float v = SCMOS ? vv[t] : 0.f;
-                    const float mu = fmaf(npx, py[t], bg);
-                    float cf, df;
-                    likelihood_terms<SCMOS>(d, v, mu, cf, df);
-                    const int h = t & 1;
-                    A[h] = fmaf(py[t], cf, A[h]);
-                    B[h] = fmaf(py2[t], df, B[h]);
-                    E[h] += cf;
-                    F[h] += df;
-                    C[t] = fmaf(xp, cf, C[t]);
-                    D[t] = fmaf(xp2, df, D[t]);
-                    if (CROSS) Gc[h] = fmaf(aG[t], df, Gc[h]);
-                }
-                col_terms<MODEL, P>(gs, hs, xp, xd1, xd2, xs1, xs2, A[0] + A[1], B[0] + B[1],
-                                    E[0] + E[1], F[0] + F[1], Gc[0] + Gc[1], ax, aw);
-                if (PIPE && j < BOX) {
-                    tmem_ld_wait<LW>(nv);
+                    for (int t = 0; t < BOX; t++) {
+                        const float d = col[t];
+                        const float v = SCMOS ? vv[t] : 0.f;
+                        const float mu = fmaf(npx, py[t], bg);
+                        float cf, df;
+                        if constexpr (UNCAPPED) likelihood_terms_uncapped(d, mu, cf, df);
+                        else likelihood_terms<SCMOS>(d, v, mu, cf, df);
+                        const int h = t & 1;
+                        A[h] = fmaf(py[t], cf, A[h]);
+                        B[h] = fmaf(py2[t], df, B[h]);
+                        E[h] += cf;
+                        F[h] += df;
+                        C[t] = fmaf(xp, cf, C[t]);
+                        D[t] = fmaf(xp2, df, D[t]);
+                        if (CROSS) Gc[h] = fmaf(aG[t], df, Gc[h]);
+                    }
+                    col_terms<MODEL, P>(gs, hs, xp, xd1, xd2, xs1, xs2, A[0] + A[1], B[0] + B[1],
+                                        E[0] + E[1], F[0] + F[1], Gc[0] + Gc[1], ax, aw);
+                    if (PIPE && j < BOX) {
+                        tmem_ld_wait<LW>(nv);
 #pragma unroll
-                    for (int q = 0; q < LW; q++) vv[q] = nv[q];
+                        for (int q = 0; q < LW; q++) vv[q] = nv[q];
+                    }
+                    xp = nxp; xd1 = nxd1; xd2 = nxd2; xs1 = nxs1; xs2 = nxs2;
                 }
-                xp = nxp; xd1 = nxd1; xd2 = nxd2; xs1 = nxs1; xs2 = nxs2;
+            };
+            if constexpr (!SCMOS) {
+                // one decision per warp (empty slots do not hold it back)
+                if (__all_sync(0xffffffffu, g >= nroi || uncapped(N, bg, dmax)))
+                    columns(std::true_type{});
+                else
+                    columns(std::false_type{});
+            } else {
+                columns(std::false_type{});
             }
 #pragma unroll
             for (int t = 0; t < BOX; t++)
@@ -1666,13 +1771,27 @@ __global__ void __launch_bounds__(128) fit_kernel_r1(const KernelArgs a, const T
 
 // ---- kernel 2: several threads per ROI ------------------------------------------
 //
-// `tpr` lanes (2..32, a power of two) share a ROI: lane r owns a contiguous
-// block of pixel columns and of y-table rows; the group shares the y tables
-// through shared memory and combines its partial sums with warp shuffles.
-// Used for batches too small to fill the GPU with one thread per ROI.
-//
-// fit_rois_tpr fits ROIs [roi0, roi0 + nroi) of `a` (nroi <= blockDim.x / tpr).
-template <int MODEL, int BOX, bool SCMOS>
+// For batches too small to fill the GPU with one thread per ROI.  TPR lanes
+// (2, 4 or 8) of one warp share a ROI as a grid of NCX column blocks by NRY
+// row blocks (2 x 1, 2 x 2, 4 x 2): lane (rx, ry) owns columns
+// [rx BOX / NCX, (rx + 1) BOX / NCX) and rows [ry BOX / NRY, (ry + 1) BOX / NRY)
+// of the ROI, evaluates the edge tables of its own columns and rows only, and
+// sums its own pixels.  The column and row terms of the gradient and Hessian
+// (col_terms, row_terms) and the Fisher column terms (fisher_column) are
+// linear in the per-column and per-row sums, so each lane applies them to its
+// partial sums, and only the 2P gradient and Hessian values (and, once, the
+// Fisher matrix and the log-likelihood) are combined across the lanes, by
+// warp shuffles.  Every lane then takes the same Newton step, so theta stays
+// identical in all of them.  The initial estimate is computed by every lane
+// from the staged ROI, in the reference's order.
+template <int TPR> struct LaneGrid {
+    static_assert(TPR == 2 || TPR == 4 || TPR == 8, "2, 4 or 8 lanes per ROI");
+    static constexpr int NCX = TPR == 2 ? 2 : TPR == 4 ? 2 : 4;
+    static constexpr int NRY = TPR / NCX;
+};
+
+// fit_rois_tpr fits ROIs [roi0, roi0 + nroi) of `a` (nroi <= blockDim.x / TPR).
+template <int MODEL, int BOX, bool SCMOS, int TPR>
 __device__ __forceinline__ void fit_rois_tpr(const KernelArgs &a, int64_t roi0, int nroi,
                                              float *smem)
 {
@@ -1680,35 +1799,48 @@ __device__ __forceinline__ void fit_rois_tpr(const KernelArgs &a, int64_t roi0, 
     constexpr bool SIG = ModelInfo<MODEL>::SIG;
     constexpr bool CROSS = (MODEL == 1 || MODEL == 3);
     constexpr int B2 = BOX * BOX;
-    constexpr int NT = ntables<MODEL>();
     constexpr int PS = SCMOS ? 2 : 1;
     constexpr int NB = SIG ? 4 : 3;
+    constexpr int NCX = LaneGrid<TPR>::NCX, NRY = LaneGrid<TPR>::NRY;
+    constexpr int RMAX = (BOX + NRY - 1) / NRY;  // rows of the largest row block
     using S = Slots<MODEL>;
 
-    const int tpr = a.tpr;
-    const int R = blockDim.x / tpr;
+    const int R = blockDim.x / TPR;
     float *spix = smem;
     int *sok = reinterpret_cast<int *>(spix + R * B2 * PS + (SCMOS ? 2 * R : 0));
-    float *sytab = reinterpret_cast<float *>(sok + R);
     stage_block<BOX, SCMOS>(a, spix, sok, R, roi0, nroi);
 
-    const int g = threadIdx.x / tpr;  // ROI slot in the block
-    const int r = threadIdx.x - g * tpr;
-    const int lane = threadIdx.x & 31;
-    const int leader = lane & ~(tpr - 1);
-    // this lane's contiguous block of pixel columns (and of y-table rows)
-    const int b0 = (r * BOX) / tpr, b1 = ((r + 1) * BOX) / tpr;
+    const int g = threadIdx.x / TPR;  // ROI slot in the block
+    const int r = threadIdx.x - g * TPR;
+    const int rx = r % NCX, ry = r / NCX;
+    const int c0 = (rx * BOX) / NCX, c1 = ((rx + 1) * BOX) / NCX;  // columns [c0, c1)
+    const int r0 = (ry * BOX) / NRY;
+    const int nr = ((ry + 1) * BOX) / NRY - r0;                     // rows [r0, r0 + nr)
     if (__all_sync(0xffffffffu, g >= nroi)) return;
     const bool valid = g < nroi && sok[g];
     const float *pix = spix + g * B2 * PS;
-    float *ytab = sytab + g * NT * BOX;
+    // the lane's last row slot holds a row only when its block is a full RMAX
+    const bool last_row = nr == RMAX;
 
     float th[P];
 #pragma unroll
     for (int k = 0; k < P; k++) th[k] = 0.f;
-    if (r == 0) initialize<MODEL, BOX, PS>(pix, a.psf, th);
+    initialize<MODEL, BOX, PS>(pix, a.psf, th);
+    // Poisson: the largest pixel of the ROI (NaN if any is NaN), for uncapped()
+    float dmax = 0.f;
+    if (!SCMOS) {
+        dmax = -INFINITY;
+        for (int j = c0; j < c1; j++)
+            for (int t = 0; t < nr; t++) {
+                const float d = pix[j * BOX + r0 + t];
+                dmax = (d > dmax || d != d) ? d : dmax;
+            }
 #pragma unroll
-    for (int k = 0; k < P; k++) th[k] = __shfl_sync(0xffffffffu, th[k], leader);
+        for (int off = TPR >> 1; off > 0; off >>= 1) {
+            const float o = __shfl_xor_sync(0xffffffffu, dmax, off);
+            dmax = (o > dmax || o != o) ? o : dmax;
+        }
+    }
 
     for (int it = 0; it <= a.iterations; ++it) {
         const bool final_pass = (it == a.iterations);
@@ -1719,108 +1851,109 @@ __device__ __forceinline__ void fit_rois_tpr(const KernelArgs &a, int64_t roi0, 
         const Axis ax = make_axis(th[S::IX], sxw, N, a.sqrt2pi, SIG);
         const Axis ay = make_axis(th[S::IY], syw, N, a.sqrt2pi, SIG);
 
-        // y-axis (row) tables: each lane walks its block of rows; shared memory
-        if (b0 < b1) {
-            EdgeWalk wy = walk_start(b0 + 1, ay);
-            for (int t = b0; t < b1; t++) {
-                float p, d1, d2, s1 = 0.f, s2 = 0.f;
-                walk_entry<SIG, true>(t + 1, ay, wy, p, d1, d2, s1, s2);
-                ytab[t] = p;
-                ytab[BOX + t] = d1;
-                ytab[2 * BOX + t] = d2;
-                if (SIG) { ytab[3 * BOX + t] = s1; ytab[4 * BOX + t] = s2; }
+        // this lane's rows of the y tables (slot t: row r0 + t + 1; a slot
+        // past the block is evaluated but not used)
+        float py[RMAX], yd1[RMAX], yd2[RMAX], ys1[SIG ? RMAX : 1], ys2[SIG ? RMAX : 1];
+        {
+            EdgeWalk wy = walk_start(r0 + 1, ay);
+#pragma unroll
+            for (int t = 0; t < RMAX; t++) {
+                float s1 = 0.f, s2 = 0.f;
+                walk_entry<SIG, true>(r0 + t + 1, ay, wy, py[t], yd1[t], yd2[t], s1, s2);
+                if (SIG) { ys1[t] = s1; ys2[t] = s2; }
             }
         }
-        __syncwarp();
-        float py[BOX];
-#pragma unroll
-        for (int t = 0; t < BOX; t++) py[t] = ytab[t];
-        EdgeWalk wx = walk_start(b0 + 1, ax);
+        EdgeWalk wx = walk_start(c0 + 1, ax);
 
         if (!final_pass) {
-            float py2[BOX], aG[CROSS ? BOX : 1], C[BOX], D[BOX];
+            float py2[RMAX], aG[CROSS ? RMAX : 1], C[RMAX], D[RMAX];
 #pragma unroll
-            for (int t = 0; t < BOX; t++) {
+            for (int t = 0; t < RMAX; t++) {
                 py2[t] = py[t] * py[t];
-                if (CROSS) aG[t] = py[t] * ytab[3 * BOX + t];
+                if (CROSS) aG[t] = py[t] * ys1[t];
                 C[t] = 0.f;
                 D[t] = 0.f;
             }
             float gs[P], hs[P];
 #pragma unroll
             for (int k = 0; k < P; k++) { gs[k] = 0.f; hs[k] = 0.f; }
-            for (int j = b0 + 1; j <= b1; j++) {
-                float xp, xd1, xd2, xs1 = 0.f, xs2 = 0.f;
-                walk_entry<SIG, true>(j, ax, wx, xp, xd1, xd2, xs1, xs2);
-                const float npx = N * xp, xp2 = xp * xp;
-                const float *col = pix + (j - 1) * BOX * PS;
-                // even and odd rows in separate partial sums: two independent
-                // FMA chains of box/2 instead of one of box
-                float A[2] = {0.f, 0.f}, B[2] = {0.f, 0.f}, E[2] = {0.f, 0.f},
-                      F[2] = {0.f, 0.f}, Gc[2] = {0.f, 0.f};
+            auto columns = [&](auto uncapped_tag) {
+                constexpr bool UNCAPPED = decltype(uncapped_tag)::value;
+                for (int j = c0 + 1; j <= c1; j++) {
+                    float xp, xd1, xd2, xs1 = 0.f, xs2 = 0.f;
+                    walk_entry<SIG, true>(j, ax, wx, xp, xd1, xd2, xs1, xs2);
+                    const float npx = N * xp, xp2 = xp * xp;
+                    const float *col = pix + ((j - 1) * BOX + r0) * PS;
+                    float A[2] = {0.f, 0.f}, B[2] = {0.f, 0.f}, E[2] = {0.f, 0.f},
+                          F[2] = {0.f, 0.f}, Gc[2] = {0.f, 0.f};
 #pragma unroll
-                for (int t = 0; t < BOX; t++) {
-                    float d, v = 0.f;
-                    if (SCMOS) {
-                        const float2 q = reinterpret_cast<const float2 *>(col)[t];
-                        d = q.x; v = q.y;
-                    } else {
-                        d = col[t];
+                    for (int t = 0; t < RMAX; t++) {
+                        if (t == RMAX - 1 && !last_row) break;
+                        float d, v = 0.f;
+                        if (SCMOS) {
+                            const float2 q = reinterpret_cast<const float2 *>(col)[t];
+                            d = q.x; v = q.y;
+                        } else {
+                            d = col[t];
+                        }
+                        const float mu = fmaf(npx, py[t], bg);
+                        float cf, df;
+                        if constexpr (UNCAPPED) likelihood_terms_uncapped(d, mu, cf, df);
+                        else likelihood_terms<SCMOS>(d, v, mu, cf, df);
+                        const int h = t & 1;
+                        A[h] = fmaf(py[t], cf, A[h]);
+                        B[h] = fmaf(py2[t], df, B[h]);
+                        E[h] += cf;
+                        F[h] += df;
+                        C[t] = fmaf(xp, cf, C[t]);
+                        D[t] = fmaf(xp2, df, D[t]);
+                        if (CROSS) Gc[h] = fmaf(aG[t], df, Gc[h]);
                     }
-                    const float mu = fmaf(npx, py[t], bg);
-                    float cf, df;
-                    likelihood_terms<SCMOS>(d, v, mu, cf, df);
-                    const int h = t & 1;
-                    A[h] = fmaf(py[t], cf, A[h]);
-                    B[h] = fmaf(py2[t], df, B[h]);
-                    E[h] += cf;
-                    F[h] += df;
-                    C[t] = fmaf(xp, cf, C[t]);
-                    D[t] = fmaf(xp2, df, D[t]);
-                    if (CROSS) Gc[h] = fmaf(aG[t], df, Gc[h]);
+                    col_terms<MODEL, P>(gs, hs, xp, xd1, xd2, xs1, xs2, A[0] + A[1],
+                                        B[0] + B[1], E[0] + E[1], F[0] + F[1], Gc[0] + Gc[1],
+                                        ax, aw);
                 }
-                col_terms<MODEL, P>(gs, hs, xp, xd1, xd2, xs1, xs2, A[0] + A[1], B[0] + B[1],
-                                    E[0] + E[1], F[0] + F[1], Gc[0] + Gc[1], ax, aw);
+            };
+            if constexpr (!SCMOS) {
+                if (__all_sync(0xffffffffu, g >= nroi || uncapped(N, bg, dmax)))
+                    columns(std::true_type{});
+                else
+                    columns(std::false_type{});
+            } else {
+                columns(std::false_type{});
+            }
+#pragma unroll
+            for (int t = 0; t < RMAX; t++) {
+                if (t == RMAX - 1 && !last_row) break;
+                row_terms<MODEL, P>(gs, hs, yd1[t], yd2[t], SIG ? ys1[t] : 0.f,
+                                    SIG ? ys2[t] : 0.f, C[t], D[t], ay, aw);
             }
 #pragma unroll
             for (int k = 0; k < P; k++) {
-                gs[k] = group_sum(gs[k], tpr);
-                hs[k] = group_sum(hs[k], tpr);
+                gs[k] = group_sum(gs[k], TPR);
+                hs[k] = group_sum(hs[k], TPR);
             }
-#pragma unroll
-            for (int t = 0; t < BOX; t++) {
-                const float Ct = group_sum(C[t], tpr), Dt = group_sum(D[t], tpr);
-                row_terms<MODEL, P>(gs, hs, ytab[BOX + t], ytab[2 * BOX + t],
-                                    SIG ? ytab[3 * BOX + t] : 0.f, SIG ? ytab[4 * BOX + t] : 0.f,
-                                    Ct, Dt, ay, aw);
-            }
-            __syncwarp();  // y-tables are rewritten by the next iteration
             newton_step<P>(th, gs, hs, a);
         } else {
-            float yd1r[BOX], ys1r[SIG ? BOX : 1];
-#pragma unroll
-            for (int t = 0; t < BOX; t++) {
-                yd1r[t] = ytab[BOX + t];
-                if (SIG) ys1r[t] = ytab[3 * BOX + t];
-            }
             float llr = 0.f;
             float Fh[P][P], Fl[P][P];
 #pragma unroll
             for (int k = 0; k < P; k++)
 #pragma unroll
                 for (int l = 0; l < P; l++) { Fh[k][l] = 0.f; Fl[k][l] = 0.f; }
-            for (int j = b0 + 1; j <= b1; j++) {
+            for (int j = c0 + 1; j <= c1; j++) {
                 float xp, xd1, xd2, xs1 = 0.f, xs2 = 0.f;
                 walk_entry<SIG, false>(j, ax, wx, xp, xd1, xd2, xs1, xs2);
                 const float npx = N * xp;
-                const float *col = pix + (j - 1) * BOX * PS;
+                const float *col = pix + ((j - 1) * BOX + r0) * PS;
                 float Q[NB][NB];
 #pragma unroll
                 for (int p = 0; p < NB; p++)
 #pragma unroll
                     for (int q = 0; q < NB; q++) Q[p][q] = 0.f;
 #pragma unroll
-                for (int t = 0; t < BOX; t++) {
+                for (int t = 0; t < RMAX; t++) {
+                    if (t == RMAX - 1 && !last_row) break;
                     float d, v = 0.f;
                     if (SCMOS) {
                         const float2 q = reinterpret_cast<const float2 *>(col)[t];
@@ -1829,18 +1962,18 @@ __device__ __forceinline__ void fit_rois_tpr(const KernelArgs &a, int64_t roi0, 
                         d = col[t];
                     }
                     const float mu = fmaf(npx, py[t], bg);
-                    final_pixel<SCMOS, SIG, NB>(d, v, mu, py[t], yd1r[t], SIG ? ys1r[t] : 0.f,
+                    final_pixel<SCMOS, SIG, NB>(d, v, mu, py[t], yd1[t], SIG ? ys1[t] : 0.f,
                                                 llr, Q);
                 }
                 fisher_column<MODEL, P, NB>(Fh, Fl, Q, xp, xd1, xs1, aw);
             }
-            llr = group_sum(llr, tpr);
+            llr = group_sum(llr, TPR);
             double Fm[P][P];
 #pragma unroll
             for (int k = 0; k < P; k++)
 #pragma unroll
                 for (int l = k; l < P; l++) {
-                    dd_group_sum(Fh[k][l], Fl[k][l], tpr);
+                    dd_group_sum(Fh[k][l], Fl[k][l], TPR);
                     Fm[k][l] = dd_to_double(Fh[k][l], Fl[k][l]);
                     Fm[l][k] = Fm[k][l];
                 }
@@ -1849,23 +1982,24 @@ __device__ __forceinline__ void fit_rois_tpr(const KernelArgs &a, int64_t roi0, 
     }
 }
 
-template <int MODEL, int BOX, bool SCMOS, bool TABLE>
+// TABLE as for fit_kernel_r1; the launch's lanes per ROI are TPR (a.tpr).
+template <int MODEL, int BOX, bool SCMOS, bool TABLE, int TPR>
 __global__ void __launch_bounds__(256) fit_kernel(const KernelArgs a, const TileTable t)
 {
     extern __shared__ __align__(16) float smem[];
-    const int R = blockDim.x / a.tpr;
+    const int R = blockDim.x / TPR;
     if (!TABLE) {
         const int64_t roi0 = (int64_t)blockIdx.x * R;
         const int64_t left = a.n - roi0;
-        fit_rois_tpr<MODEL, BOX, SCMOS>(a, roi0, left < R ? (int)left : R, smem);
+        fit_rois_tpr<MODEL, BOX, SCMOS, TPR>(a, roi0, left < R ? (int)left : R, smem);
         return;
     }
-    TableSlot *ts = table_slot(smem, smem_bytes(MODEL, BOX, SCMOS, a.tpr, R));
+    TableSlot *ts = table_slot(smem, smem_bytes(MODEL, BOX, SCMOS, TPR, R));
     table_slot_init(ts);
     int64_t roi0;
     int nroi;
     for (int k = 0; table_next(t, R, ts, k, roi0, nroi); k++) {
-        fit_rois_tpr<MODEL, BOX, SCMOS>(ts->a, roi0, nroi, smem);
+        fit_rois_tpr<MODEL, BOX, SCMOS, TPR>(ts->a, roi0, nroi, smem);
         __syncthreads();  // the tile's shared memory and slot are free again
     }
 }

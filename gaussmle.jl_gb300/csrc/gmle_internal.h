@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/gaussmle_gb300.h"
+#include "gmle_generic.h"
 #include "gmle_launch.cuh"
 
 namespace gmle_rt {

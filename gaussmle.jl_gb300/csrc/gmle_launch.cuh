@@ -1,7 +1,14 @@
-// gmle_launch.cuh - launch of one fit-kernel specialisation.  Each
-// gmle_fit_<model>_<camera family>.cu translation unit instantiates the
-// kernels of one PSF model and camera family for every supported box size, so
-// the eight units compile in parallel.
+// gmle_launch.cuh - launch of one fit-kernel specialisation.
+//
+// The kernels of one PSF model and camera family are compiled in three parts,
+// each its own translation unit (gmle_fit_family.cu, compiled once per
+// (model, camera family, part) with -D defines, so the 24 units compile in
+// parallel):
+//   part 0  one thread per ROI (fit_kernel_r1), odd boxes 5..15;
+//   part 1  one thread per ROI, boxes 3, 4, 6, 8, 10, 12, 14, 16;
+//   part 2  several lanes per ROI (fit_kernel): 4 and 8 lanes for odd boxes
+//           5..15, 4 lanes for the others.
+// Other translation units see the parts through extern template declarations.
 #pragma once
 
 #include <algorithm>
@@ -10,17 +17,23 @@
 
 namespace gmle {
 
-// Box sizes with a compiled specialisation (the configurations use 7..15).
-constexpr int kBoxes[] = {5, 7, 9, 11, 13, 15};
-constexpr int kNumBoxes = 6;
+// Box sizes with a compiled specialisation: every edge length 3..16 (the
+// configurations use 7..15; the reference accepts any box >= 3,
+// src/interface.jl:22).  Larger boxes run in the runtime-box kernel
+// (gmle_fit_generic.cu).
+constexpr int kMinBox = 3, kMaxBox = 16;
+constexpr int kNumBoxes = kMaxBox - kMinBox + 1;
 
 __host__ __device__ constexpr int box_index(int box)
 {
-    return box == 5 ? 0 : box == 7 ? 1 : box == 9 ? 2 : box == 11 ? 3 : box == 13 ? 4
-                                                                     : box == 15 ? 5 : -1;
+    return box >= kMinBox && box <= kMaxBox ? box - kMinBox : -1;
 }
+__host__ __device__ constexpr int box_of_index(int k) { return k + kMinBox; }
 
 inline bool box_supported(int box) { return box_index(box) >= 0; }
+
+// The part of the odd boxes 5..15 (the most used sizes, with 8-lane kernels).
+__host__ __device__ constexpr bool main_box(int box) { return box >= 5 && box <= 15 && (box & 1); }
 
 // Largest block of the one-thread-per-ROI kernel (its __launch_bounds__).
 constexpr int kMaxThreadsR1 = 128;
@@ -37,23 +50,37 @@ struct LaunchShape {
     bool lm = false;
 };
 
-#define GMLE_DECLARE_FAMILY(M, FAM)                                                           \
-    cudaError_t launch_fit_m##M##_##FAM(int box, const KernelArgs &a, const TileTable &t,     \
-                                        const LaunchShape &shape, cudaStream_t s);            \
-    int table_blocks_m##M##_##FAM(int box, int tpr, int rois_per_block);
-GMLE_DECLARE_FAMILY(0, poisson) GMLE_DECLARE_FAMILY(0, scmos)
-GMLE_DECLARE_FAMILY(1, poisson) GMLE_DECLARE_FAMILY(1, scmos)
-GMLE_DECLARE_FAMILY(2, poisson) GMLE_DECLARE_FAMILY(2, scmos)
-GMLE_DECLARE_FAMILY(3, poisson) GMLE_DECLARE_FAMILY(3, scmos)
-#undef GMLE_DECLARE_FAMILY
+// Lanes per ROI with a compiled kernel: 1 (fit_kernel_r1) for every box; 4
+// (fit_kernel) for every box; 8 for the odd boxes 5..15.
+inline bool tpr_supported(int tpr, int box)
+{
+    return tpr == 1 || tpr == 4 || (tpr == 8 && main_box(box));
+}
+
+// Part holding the kernel of a launch shape (see the top of this file).
+__host__ __device__ constexpr int part_of(int box, int tpr) { return tpr == 1 ? (main_box(box) ? 0 : 1) : 2; }
+
+template <int MODEL, bool SCMOS, int PART>
+cudaError_t launch_part(int box, const KernelArgs &a, const TileTable &t, const LaunchShape &shape,
+                        cudaStream_t s);
+template <int MODEL, bool SCMOS, int PART>
+int table_blocks_part(int box, int tpr, int rois_per_block);
 
 inline cudaError_t launch_fit(int model, int box, bool scmos, const KernelArgs &a,
                               const TileTable &t, const LaunchShape &shape, cudaStream_t s)
 {
-#define GMLE_CASE(M)                                                        \
-    case M:                                                                 \
-        return scmos ? launch_fit_m##M##_scmos(box, a, t, shape, s)         \
-                     : launch_fit_m##M##_poisson(box, a, t, shape, s);
+    if (!box_supported(box) || !tpr_supported(shape.tpr, box)) return cudaErrorInvalidValue;
+    const int part = part_of(box, shape.tpr);
+#define GMLE_CASE(M)                                                                       \
+    case M:                                                                                \
+        if (part == 0)                                                                     \
+            return scmos ? launch_part<M, true, 0>(box, a, t, shape, s)                    \
+                         : launch_part<M, false, 0>(box, a, t, shape, s);                  \
+        if (part == 1)                                                                     \
+            return scmos ? launch_part<M, true, 1>(box, a, t, shape, s)                    \
+                         : launch_part<M, false, 1>(box, a, t, shape, s);                  \
+        return scmos ? launch_part<M, true, 2>(box, a, t, shape, s)                        \
+                     : launch_part<M, false, 2>(box, a, t, shape, s);
     switch (model) {
         GMLE_CASE(0) GMLE_CASE(1) GMLE_CASE(2) GMLE_CASE(3)
         default: return cudaErrorInvalidValue;
@@ -66,10 +93,18 @@ inline cudaError_t launch_fit(int model, int box, bool scmos, const KernelArgs &
 // the current device.
 inline int table_blocks_per_sm(int model, int box, bool scmos, int tpr, int rois_per_block)
 {
-#define GMLE_CASE(M)                                                        \
-    case M:                                                                 \
-        return scmos ? table_blocks_m##M##_scmos(box, tpr, rois_per_block)  \
-                     : table_blocks_m##M##_poisson(box, tpr, rois_per_block);
+    if (!box_supported(box) || !tpr_supported(tpr, box)) return -(int)cudaErrorInvalidValue;
+    const int part = part_of(box, tpr);
+#define GMLE_CASE(M)                                                                       \
+    case M:                                                                                \
+        if (part == 0)                                                                     \
+            return scmos ? table_blocks_part<M, true, 0>(box, tpr, rois_per_block)         \
+                         : table_blocks_part<M, false, 0>(box, tpr, rois_per_block);       \
+        if (part == 1)                                                                     \
+            return scmos ? table_blocks_part<M, true, 1>(box, tpr, rois_per_block)         \
+                         : table_blocks_part<M, false, 1>(box, tpr, rois_per_block);       \
+        return scmos ? table_blocks_part<M, true, 2>(box, tpr, rois_per_block)             \
+                     : table_blocks_part<M, false, 2>(box, tpr, rois_per_block);
     switch (model) {
         GMLE_CASE(0) GMLE_CASE(1) GMLE_CASE(2) GMLE_CASE(3)
         default: return 0;
@@ -86,30 +121,45 @@ inline size_t launch_smem(int model, int box, bool scmos, int tpr, int rpb, bool
 
 using FitKernel = void (*)(const KernelArgs, const TileTable);
 
+// The kernels of a part: defined where GMLE_PART (and GMLE_PART_BOXES) are,
+// in gmle_fit_family.cu.
+#ifdef GMLE_PART
 template <int MODEL, int BOX, bool SCMOS>
 cudaError_t kernel_for(int tpr, bool table, bool lm, FitKernel *kern)
 {
+    constexpr int PART = part_of(BOX, 1) == 0 ? 0 : 1;  // this box's one-thread part
     const bool r1 = tpr == 1;
     if (lm && (!r1 || table)) return cudaErrorInvalidConfiguration;
-    *kern = lm ? fit_kernel_r1<MODEL, BOX, SCMOS, false, true>
-          : r1 ? (table ? fit_kernel_r1<MODEL, BOX, SCMOS, true> : fit_kernel_r1<MODEL, BOX, SCMOS, false>)
-               : (table ? fit_kernel<MODEL, BOX, SCMOS, true> : fit_kernel<MODEL, BOX, SCMOS, false>);
+    if (!tpr_supported(tpr, BOX)) return cudaErrorInvalidConfiguration;
+    if constexpr (GMLE_PART == PART) {
+        if (!r1) return cudaErrorInvalidConfiguration;
+        if (lm) *kern = fit_kernel_r1<MODEL, BOX, SCMOS, false, true>;
+        else *kern = table ? fit_kernel_r1<MODEL, BOX, SCMOS, true> : fit_kernel_r1<MODEL, BOX, SCMOS, false>;
+    } else if constexpr (GMLE_PART == 2) {
+        if (r1) return cudaErrorInvalidConfiguration;
+        if (tpr == 4) *kern = table ? fit_kernel<MODEL, BOX, SCMOS, true, 4> : fit_kernel<MODEL, BOX, SCMOS, false, 4>;
+        else if constexpr (main_box(BOX))
+            *kern = table ? fit_kernel<MODEL, BOX, SCMOS, true, 8> : fit_kernel<MODEL, BOX, SCMOS, false, 8>;
+    } else {
+        return cudaErrorInvalidConfiguration;
+    }
     // The largest dynamic shared memory a block may have, once per kernel and
     // device (setting it twice is harmless).
     constexpr int kMaxDevices = 64;
-    static bool done[2][2][2][kMaxDevices] = {};
+    static bool done[2][3][2][kMaxDevices] = {};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     const bool known = dev >= 0 && dev < kMaxDevices;
-    if (known && done[lm][r1][table][dev]) return cudaSuccess;
+    const int ti = tpr == 1 ? 0 : tpr == 4 ? 1 : 2;
+    if (known && done[lm][ti][table][dev]) return cudaSuccess;
     // the 227 KiB a block may use include the kernel's static shared memory
     cudaFuncAttributes fa;
     e = cudaFuncGetAttributes(&fa, *kern);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(*kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              227 * 1024 - (int)fa.sharedSizeBytes);
-    if (e == cudaSuccess && known) done[lm][r1][table][dev] = true;
+    if (e == cudaSuccess && known) done[lm][ti][table][dev] = true;
     return e;
 }
 
@@ -181,34 +231,45 @@ int table_blocks_one(int tpr, int rpb)
     return tmem_kernel_blocks_per_sm(kern, rpb * tpr, smem, tmem_var_cols(BOX));
 }
 
-#define GMLE_BOX_SWITCH(CALL)       \
-    switch (box) {                  \
-        case 5: CALL(5)             \
-        case 7: CALL(7)             \
-        case 9: CALL(9)             \
-        case 11: CALL(11)           \
-        case 13: CALL(13)           \
-        case 15: CALL(15)           \
-        default: break;             \
-    }
+#define GMLE_CASE_PART0(CALL) CALL(5) CALL(7) CALL(9) CALL(11) CALL(13) CALL(15)
+#define GMLE_CASE_PART1(CALL) CALL(3) CALL(4) CALL(6) CALL(8) CALL(10) CALL(12) CALL(14) CALL(16)
+#define GMLE_CASE_PART2(CALL) GMLE_CASE_PART0(CALL) GMLE_CASE_PART1(CALL)
 
-template <int MODEL, bool SCMOS>
-cudaError_t launch_family(int box, const KernelArgs &a, const TileTable &t,
-                          const LaunchShape &shape, cudaStream_t s)
+template <int MODEL, bool SCMOS, int PART>
+cudaError_t launch_part(int box, const KernelArgs &a, const TileTable &t, const LaunchShape &shape,
+                        cudaStream_t s)
 {
-#define GMLE_CASE(B) return launch_one<MODEL, B, SCMOS>(a, t, shape, s);
-    GMLE_BOX_SWITCH(GMLE_CASE)
+#define GMLE_CASE(B) case B: return launch_one<MODEL, B, SCMOS>(a, t, shape, s);
+    switch (box) {
+        GMLE_PART_BOXES(GMLE_CASE)
+        default: break;
+    }
 #undef GMLE_CASE
     return cudaErrorInvalidValue;
 }
 
-template <int MODEL, bool SCMOS>
-int table_blocks_family(int box, int tpr, int rpb)
+template <int MODEL, bool SCMOS, int PART>
+int table_blocks_part(int box, int tpr, int rpb)
 {
-#define GMLE_CASE(B) return table_blocks_one<MODEL, B, SCMOS>(tpr, rpb);
-    GMLE_BOX_SWITCH(GMLE_CASE)
+#define GMLE_CASE(B) case B: return table_blocks_one<MODEL, B, SCMOS>(tpr, rpb);
+    switch (box) {
+        GMLE_PART_BOXES(GMLE_CASE)
+        default: break;
+    }
 #undef GMLE_CASE
     return 0;
 }
+#endif
+
+#define GMLE_EXTERN_PART(M, S, P)                                                            \
+    extern template cudaError_t launch_part<M, S, P>(int, const KernelArgs &, const TileTable &, \
+                                                     const LaunchShape &, cudaStream_t);      \
+    extern template int table_blocks_part<M, S, P>(int, int, int);
+#define GMLE_EXTERN_MODEL(M)                                                         \
+    GMLE_EXTERN_PART(M, false, 0) GMLE_EXTERN_PART(M, false, 1) GMLE_EXTERN_PART(M, false, 2) \
+    GMLE_EXTERN_PART(M, true, 0) GMLE_EXTERN_PART(M, true, 1) GMLE_EXTERN_PART(M, true, 2)
+GMLE_EXTERN_MODEL(0) GMLE_EXTERN_MODEL(1) GMLE_EXTERN_MODEL(2) GMLE_EXTERN_MODEL(3)
+#undef GMLE_EXTERN_MODEL
+#undef GMLE_EXTERN_PART
 
 }  // namespace gmle

@@ -11,24 +11,30 @@
 // array g_noalloc_scratch, reserved on a device when this module is loaded
 // there and held until the process exits:
 //
-//   [0, 512)       unsigned long long counters[64]: the tile counters of the
-//                  48 kinds, then the skipped-ROI counter.  A tile counter must
-//                  be zero when its launch starts; every call's table copy
-//                  writes all of them to zero, on the caller's stream, before
-//                  its launches.
-//   [512, 1536)    int64_t headers[48][2]: {groups, tiles} of each launch.
-//   [1536, 9728)   int64_t tile0[GMLE_NOALLOC_MAX_GROUPS]: each group's first
+//   [0, 1024)      unsigned long long counters[128]: the tile counters of the
+//                  112 kinds (2 camera families x 4 models x boxes 3..16),
+//                  then the skipped-ROI counter.  A tile counter must be zero
+//                  when its launch starts; every call's table write sets all
+//                  of them to zero, on the caller's stream, before its
+//                  launches.
+//   [1024, 3072)   int64_t headers[112][2]: {groups, tiles} of each launch.
+//   [3072, 11264)  int64_t tile0[GMLE_NOALLOC_MAX_GROUPS]: each group's first
 //                  tile within its launch (the tile's group is found by
 //                  binary search, so no per-tile table is needed).
-//   [9728, ...)    gmle::KernelArgs args[GMLE_NOALLOC_MAX_GROUPS].
+//   [11264, ...)   gmle::KernelArgs args[GMLE_NOALLOC_MAX_GROUPS].
 // Each launch reads its own contiguous slice of tile0 and args.
 //
-// A call builds the image of [0, 9728 + 224 * groups) in a static host buffer,
-// copies it with one cudaMemcpyAsync on the caller's stream (the pageable
-// source is consumed before that call returns, so the buffer is reused by the
-// next call), then enqueues the launches on the same stream.  It allocates
-// nothing: no cudaMalloc, cudaMallocHost, cudaFree, stream or event, and no
-// host heap.
+// A call builds the image of [0, 11264 + 224 * groups) in a static host buffer,
+// then writes it into the scratch with write_scratch launches on the caller's
+// stream that carry it in their launch parameters, up to 32 704 bytes each
+// (one launch for up to 95 groups, eight for 1024).  Launch parameters are
+// copied when a launch is enqueued, so the host buffer is free for the next
+// call as soon as this one returns, and nothing waits for the stream: a
+// host-to-device copy from the (pageable) buffer could instead make the host
+// wait for the stream's earlier work, and would read the buffer again if its
+// stream work were replayed.  The fit launches follow on the same stream.  It
+// allocates nothing: no cudaMalloc, cudaMallocHost, cudaFree, stream or event,
+// and no host heap.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -47,8 +53,8 @@ using gmle_rt::kKinds;
 constexpr int kMaxGroups = GMLE_NOALLOC_MAX_GROUPS;
 constexpr size_t kCountersOff = 0;
 constexpr int kBadCounter = kKinds;  // index in counters[]
-constexpr size_t kHeadersOff = 512;
-constexpr size_t kTile0Off = 1536;
+constexpr size_t kHeadersOff = 1024;
+constexpr size_t kTile0Off = 3072;
 constexpr size_t kArgsOff = kTile0Off + sizeof(int64_t) * kMaxGroups;
 constexpr size_t kScratchBytes = kArgsOff + sizeof(KernelArgs) * kMaxGroups;
 constexpr int kMaxDevices = 64;
@@ -60,8 +66,27 @@ static_assert(sizeof(KernelArgs) % 16 == 0 && kArgsOff % 16 == 0, "16-byte align
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-// Host image of the scratch, and per-device set-up; both under g_mu.
+// One piece of the host image, carried in a launch's parameters (kernel
+// parameters may take up to 32 764 bytes).
+constexpr int kChunkBytes = 32704;
+struct ScratchChunk {
+    uint32_t offset;  // into the scratch, a multiple of 16
+    uint32_t bytes;   // a multiple of 16, at most kChunkBytes
+    uint32_t pad[2];
+    uint4 data[kChunkBytes / 16];
+};
+static_assert(sizeof(ScratchChunk) <= 32764, "kernel parameter limit");
+
+__global__ void write_scratch(const ScratchChunk c)
+{
+    uint4 *dst = reinterpret_cast<uint4 *>(g_noalloc_scratch + c.offset);
+    for (uint32_t w = threadIdx.x; w < c.bytes / 16; w += blockDim.x) dst[w] = c.data[w];
+}
+
+// Host image of the scratch, the launch parameters of its pieces, and
+// per-device set-up; all under g_mu.
 alignas(256) unsigned char g_stage[kScratchBytes];
+ScratchChunk g_chunk;
 int g_order[kMaxGroups];
 std::mutex g_mu;
 struct DeviceState {
@@ -96,7 +121,8 @@ gmle_status check_group(const gmle_group &G, int k, bool have_var, bool have_adu
                       d.model);
     if (!gmle::box_supported(d.box))
         return report(err, err_len, GMLE_UNSUPPORTED_BOX,
-                      "group %d: box size %d has no compiled kernel (5..15 odd)", k, d.box);
+                      "group %d: box size %d: this entry point takes boxes %d..%d", k, d.box,
+                      gmle::kMinBox, gmle::kMaxBox);
     if (d.iterations < 0) return report(err, err_len, GMLE_INVALID_ARG, "group %d: iterations < 0", k);
     if (d.camera < 0 || d.camera > 2)
         return report(err, err_len, GMLE_INVALID_ARG, "group %d: unknown camera id %d", k, d.camera);
@@ -247,14 +273,21 @@ extern "C" gmle_status gmle_fit_mixed_device_noalloc(const gmle_group *groups, i
     if (used == 0) return GMLE_OK;
 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    e = cudaMemcpyAsync(S.scratch, g_stage, kArgsOff + sizeof(KernelArgs) * (size_t)used,
-                        cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) return cuda_report(err, err_len, e, "H2D group tables");
+    const size_t image = kArgsOff + sizeof(KernelArgs) * (size_t)used;
+    for (size_t off = 0; off < image; off += kChunkBytes) {
+        const size_t b = std::min<size_t>(kChunkBytes, image - off);
+        g_chunk.offset = (uint32_t)off;
+        g_chunk.bytes = (uint32_t)b;
+        std::memcpy(g_chunk.data, g_stage + off, b);
+        write_scratch<<<1, 256, 0, s>>>(g_chunk);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_report(err, err_len, e, "group table write");
+    }
     for (int kind = 0; kind < kKinds; kind++) {
         if (h_headers[2 * kind] == 0) continue;
         const KernelArgs &A0 = h_args[first[kind]];
         const int model = (kind / gmle::kNumBoxes) % 4;
-        const int box = gmle::kBoxes[kind % gmle::kNumBoxes];
+        const int box = gmle::box_of_index(kind % gmle::kNumBoxes);
         const bool scmos = kind >= kKinds / 2;
         gmle::TileTable t;
         t.header = reinterpret_cast<const int64_t *>(S.scratch + kHeadersOff) + 2 * kind;

@@ -55,9 +55,13 @@ gmle_status check_desc(gmle_ctx *ctx, const gmle_fit_desc *d)
     if (!d) return fail(ctx, GMLE_INVALID_ARG, "desc is NULL");
     if (d->model < 0 || d->model > 3)
         return fail(ctx, GMLE_UNSUPPORTED_MODEL, "unknown model id %d", d->model);
-    if (!gmle::box_supported(d->box))
-        return fail(ctx, GMLE_UNSUPPORTED_BOX, "box size %d has no compiled kernel (5..15 odd)",
-                    d->box);
+    if (!gmle::box_supported(d->box) && !gmle::generic_box(d->box))
+        return fail(ctx, GMLE_UNSUPPORTED_BOX, "box size %d: ROIs of %d..%d pixels are supported",
+                    d->box, gmle::kMinBox, gmle::kGenericMaxBox);
+    if (gmle::generic_box(d->box) && d->method != GMLE_METHOD_NEWTON)
+        return fail(ctx, GMLE_UNSUPPORTED_BOX,
+                    "box size %d: the full-Hessian method takes boxes %d..%d", d->box,
+                    gmle::kMinBox, gmle::kMaxBox);
     if (d->iterations < 0) return fail(ctx, GMLE_INVALID_ARG, "iterations < 0");
     if (d->camera < 0 || d->camera > 2)
         return fail(ctx, GMLE_INVALID_ARG, "unknown camera id %d", d->camera);
@@ -89,9 +93,7 @@ Tuning default_tuning(int num_sms, int model, int box, bool scmos, int64_t n)
     const int64_t rois_per_sm = (int64_t)((200 * 1024) / per_roi);
     const int64_t want_threads_sm = 512;
     int tpr = 1;
-    while (tpr < 4 && (rois_per_sm * tpr < want_threads_sm ||
-                       n * tpr < (int64_t)num_sms * want_threads_sm))
-        tpr *= 2;
+    if (rois_per_sm < want_threads_sm || n < (int64_t)num_sms * want_threads_sm) tpr = 4;
     // one thread per ROI with sCMOS data: blocks of 4 warps use the tensor
     // memory that holds the variance tiles fully
     int rpb = tpr == 1 ? (scmos ? 128 : 32) : 128 / tpr;
@@ -107,6 +109,7 @@ namespace gmle_rt {
 Tuning pick_tuning(gmle_ctx *ctx, const gmle_fit_desc *d, int64_t n)
 {
     const bool scmos = d->camera != GMLE_CAMERA_POISSON;
+    if (gmle::generic_box(d->box)) return {1, gmle::generic_rois_per_block(d->box, scmos)};
     auto it = ctx->tuning.find({d->model, d->box, (int)scmos});
     Tuning t = it != ctx->tuning.end() ? it->second
                                        : default_tuning(ctx->num_sms, d->model, d->box, scmos, n);
@@ -160,6 +163,7 @@ cudaError_t launch(gmle_ctx *ctx, const gmle_fit_desc *d, const KernelArgs &a, i
 {
     const bool scmos = d->camera != GMLE_CAMERA_POISSON;
     ctx->launches++;
+    if (gmle::generic_box(d->box)) return gmle::launch_fit_generic(d->model, d->box, scmos, a, s);
     gmle::LaunchShape shape{a.tpr, rpb, 0};
     shape.lm = d->method == GMLE_METHOD_FISHER_LM;
     return gmle::launch_fit(d->model, d->box, scmos, a, gmle::TileTable{}, shape, s);
@@ -508,10 +512,12 @@ gmle_status gmle_set_tuning(gmle_ctx *ctx, int32_t model, int32_t box, int32_t c
         ctx->tuning.erase({model, box, (int)(camera != GMLE_CAMERA_POISSON)});
         return GMLE_OK;
     }
-    if (tpr < 1 || tpr > 32 || (tpr & (tpr - 1)))
-        return fail(ctx, GMLE_INVALID_ARG, "threads_per_roi must be a power of two in 1..32");
     if (model < 0 || model > 3) return fail(ctx, GMLE_UNSUPPORTED_MODEL, "unknown model");
-    if (!gmle::box_supported(box)) return fail(ctx, GMLE_UNSUPPORTED_BOX, "unsupported box");
+    if (!gmle::box_supported(box))
+        return fail(ctx, GMLE_UNSUPPORTED_BOX, "box %d has no launch-shape choice (3..16)", box);
+    if (!gmle::tpr_supported(tpr, box))
+        return fail(ctx, GMLE_INVALID_ARG,
+                    "threads_per_roi must be 1, 4, or 8 (8: odd boxes 5..15 only)");
     const bool scmos = camera != GMLE_CAMERA_POISSON;
     const int threads = tpr * rois_per_block;
     if (rois_per_block < 1 || threads > (tpr == 1 ? gmle::kMaxThreadsR1 : 256) || threads % 32)
@@ -541,6 +547,28 @@ gmle_status gmle_autotune(gmle_ctx *ctx, const gmle_fit_desc *desc, const float 
         return fail(ctx, GMLE_INVALID_ARG, "sCMOS fit needs ROI corners");
     cudaSetDevice(ctx->device);
     const bool scmos = desc->camera != GMLE_CAMERA_POISSON;
+    if (gmle::generic_box(desc->box)) {
+        // one launch shape: the run-time-box kernel's
+        const Tuning t = pick_tuning(ctx, desc, n);
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0), "cudaEventCreate");
+        CK(cudaEventCreate(&e1), "cudaEventCreate");
+        KernelArgs a = make_args(ctx, desc, d_data, d_x_corners, d_y_corners, n, d_params,
+                                 d_crlb, d_llr, d_flags, 1);
+        cudaError_t e = cudaEventRecord(e0, ctx->s_fit);
+        if (e == cudaSuccess) e = launch(ctx, desc, a, t.rois_per_block, ctx->s_fit);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->s_fit);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "autotune launch");
+        if (threads_per_roi) *threads_per_roi = 1;
+        if (rois_per_block) *rois_per_block = t.rois_per_block;
+        if (ms_per_fit) *ms_per_fit = ms;
+        return GMLE_OK;
+    }
     // shapes are kept per (model, box, camera family) and timed with the
     // reference's method, which runs in every shape
     gmle_fit_desc dn = *desc;
@@ -555,7 +583,8 @@ gmle_status gmle_autotune(gmle_ctx *ctx, const gmle_fit_desc *desc, const float 
     // (three warps: two such blocks of large sCMOS ROIs fit where one of four
     // warps does)
     static const int kThreads[] = {32, 64, 96, 128, 256};
-    for (int tpr = 1; tpr <= 8; tpr *= 2) {
+    for (int tpr : {1, 4, 8}) {
+        if (!gmle::tpr_supported(tpr, desc->box)) continue;
         for (int threads : kThreads) {
             if (threads > (tpr == 1 ? gmle::kMaxThreadsR1 : 256)) continue;
             if (tpr > 1 && threads == 96) continue;
@@ -647,6 +676,11 @@ gmle_status validate_groups(gmle_ctx *ctx, const gmle_group *groups, int32_t ngr
         const gmle_group &G = groups[k];
         gmle_status st = check_desc(ctx, &G.desc);
         if (st != GMLE_OK) return st;
+        if (!gmle::box_supported(G.desc.box))
+            return fail(ctx, GMLE_UNSUPPORTED_BOX,
+                        "group %d: box size %d: mixed batches and serving take boxes %d..%d "
+                        "(larger ROIs: gmle_fit or gmle_fit_device)", k, G.desc.box,
+                        gmle::kMinBox, gmle::kMaxBox);
         if (G.n < 0) return fail(ctx, GMLE_INVALID_ARG, "group %d: n < 0", k);
         if (G.n > 0 && (!G.data || !G.params || !G.crlb || !G.llr))
             return fail(ctx, GMLE_INVALID_ARG, "group %d: data and output pointers are required", k);

@@ -36,6 +36,7 @@ EXPORTED = [
     "gmle_fit_mixed_device", "gmle_server_start", "gmle_server_stop", "gmle_submit",
     "gmle_poll", "gmle_wait", "gmle_server_stats_get", "gmle_fit_mixed_device_noalloc",
     "gmle_pvalues", "gmle_pvalues_device", "gmle_cut_rois_device", "gmle_simulate_device",
+    "gmle_math_selftest",
 ]
 
 
@@ -139,6 +140,7 @@ def load(path: str | Path | None = None) -> C.CDLL:
             "gmle_simulate_device": ([vp, vp, vp, vp, vp, i64, C.c_uint64, vp, vp], C.c_int),
             "gmle_fit_mixed_device_noalloc": ([C.POINTER(Group), i32, vp, vp, vp, i32, i32, vp,
                                                C.c_char_p, i32], C.c_int),
+            "gmle_math_selftest": ([vp, i64, vp, vp], C.c_int),
         }
         for name, (args, res) in sigs.items():
             f = getattr(lib, name)

@@ -1,8 +1,11 @@
 """Build libgaussmle_sm100a.so in-tree with nvcc for sm_103a.
 
-The library is the product: eight kernel translation units (PSF model x camera
-family) plus the C-ABI runtime, compiled in parallel (one -gencode, no cmake;
-the heaviest units first) and linked into ``<package root>/lib/libgaussmle_sm100a.so``.
+The library is the product: the fit kernels, compiled from one family source
+(csrc/gmle_fit_family.cu) as 24 units - per PSF model (4), camera family (2)
+and part (3: one thread per ROI for the odd boxes 5..15, for the other boxes
+3..16, several lanes per ROI) - plus the runtime-box kernel and the C-ABI
+runtime, compiled in parallel (one -gencode, no cmake; the heaviest units
+first) and linked into ``<package root>/lib/libgaussmle_sm100a.so``.
 """
 from __future__ import annotations
 
@@ -23,10 +26,16 @@ LIB_PATH = LIB_DIR / LIB_NAME
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2",
               f"-I{REPO_ROOT / 'include'}"]
-SOURCES = [f"gmle_fit_{m}_{cam}.cu" for m in ("astig", "xynbsxsy", "xynbs", "xynb")
-           for cam in ("poisson", "scmos")] + ["gmle_runtime.cu", "gmle_server.cu",
-                                                "gmle_noalloc.cu", "gmle_pvalue.cu",
-                                                "gmle_frames.cu", "gmle_simulate.cu"]
+# (source, object stem, extra flags); heaviest first: the one-thread parts of
+# the astigmatic and sigma models
+FAMILY = "gmle_fit_family.cu"
+_NAMES = {0: "xynb", 1: "xynbs", 2: "xynbsxsy", 3: "astig"}
+UNITS = [(FAMILY, f"gmle_fit_{_NAMES[m]}_{'scmos' if c else 'poisson'}_p{p}",
+          [f"-DGMLE_MODEL={m}", f"-DGMLE_SCMOS={c}", f"-DGMLE_PART={p}"])
+         for p in (0, 1, 2) for m in (3, 2, 1, 0) for c in (1, 0)] + \
+        [(src, Path(src).stem, []) for src in
+         ("gmle_fit_generic.cu", "gmle_runtime.cu", "gmle_server.cu", "gmle_noalloc.cu",
+          "gmle_pvalue.cu", "gmle_frames.cu", "gmle_simulate.cu", "gmle_math.cu")]
 
 
 def nvcc() -> str:
@@ -51,14 +60,15 @@ def up_to_date() -> bool:
     return all(p.stat().st_mtime <= t for p in _deps())
 
 
-def _compile(src: str, verbose: bool) -> Path:
-    obj = BUILD_DIR / (Path(src).stem + ".o")
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", str(CSRC / src), "-o", str(obj)]
+def _compile(unit, verbose: bool) -> Path:
+    src, stem, defs = unit
+    obj = BUILD_DIR / (stem + ".o")
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *defs, "-c", str(CSRC / src), "-o", str(obj)]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
-        raise RuntimeError(f"nvcc failed for {src}:\n{res.stdout}\n{res.stderr}")
+        raise RuntimeError(f"nvcc failed for {stem}:\n{res.stdout}\n{res.stderr}")
     if verbose:
         print(res.stderr)
     return obj
@@ -70,9 +80,9 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         return LIB_PATH
     BUILD_DIR.mkdir(parents=True, exist_ok=True)
     LIB_DIR.mkdir(parents=True, exist_ok=True)
-    workers = min(len(SOURCES), os.cpu_count() or 1)
+    workers = min(len(UNITS), os.cpu_count() or 1)
     with cf.ThreadPoolExecutor(max_workers=workers) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
+        objs = list(ex.map(lambda u: _compile(u, verbose), UNITS))
     tmp = LIB_PATH.with_suffix(".so.tmp")
     cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
     res = subprocess.run(cmd, capture_output=True, text=True)

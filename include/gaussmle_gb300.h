@@ -99,7 +99,8 @@ typedef enum {
  */
 typedef struct {
     int32_t model;      /* gmle_model */
-    int32_t box;        /* ROI edge length: 5, 7, 9, 11, 13 or 15 */
+    int32_t box;        /* ROI edge length 3..64 (gmle_fit, gmle_fit_device); 3..16 in
+                           mixed batches, serving and the no-allocation entry point */
     int32_t iterations; /* Newton iterations (reference default 20) */
     int32_t camera;     /* gmle_camera */
     float psf[8];
@@ -166,7 +167,9 @@ gmle_status gmle_fit_device_errors(gmle_ctx *ctx, int64_t *count);
  * Kernel launch shape used for a (model, box, camera): threads per ROI and
  * ROIs per block, as picked by the autotuner (or set by gmle_set_tuning;
  * setting (0, 0) forgets the entry and restores the size-based default).
- * One thread per ROI allows at most 64 ROIs per block.
+ * Threads per ROI: 1, 4, or 8 (8 for odd boxes 5..15 only); one thread per
+ * ROI allows at most 128 ROIs per block, several lanes 256 threads per block.
+ * Boxes 3..16; larger boxes run in one fixed shape.
  */
 gmle_status gmle_get_tuning(gmle_ctx *ctx, int32_t model, int32_t box, int32_t camera,
                             int32_t *threads_per_roi, int32_t *rois_per_block);
@@ -174,7 +177,7 @@ gmle_status gmle_set_tuning(gmle_ctx *ctx, int32_t model, int32_t box, int32_t c
                             int32_t threads_per_roi, int32_t rois_per_block);
 
 /*
- * Autotuner: times every candidate launch shape (threads per ROI 1, 2, 4, 8;
+ * Autotuner: times every candidate launch shape (threads per ROI 1, 4, 8;
  * 32..256 threads per block, within 227 KiB of shared memory) of the fit
  * kernel for `desc` on a device-resident batch, keeps the fastest for
  * (model, box, camera family) in the context and returns it with its time
@@ -238,6 +241,16 @@ gmle_status gmle_pvalues(gmle_ctx *ctx, const float *llr, int64_t n, int32_t df,
 gmle_status gmle_pvalues_device(gmle_ctx *ctx, const float *d_llr, int64_t n, int32_t df,
                                 float *d_pvalues, void *stream);
 
+/*
+ * Accuracy check of the fit kernels' own elementary functions (no reference
+ * counterpart: the reference calls SpecialFunctions.erf and Base.exp).  For
+ * each of the n device-resident arguments x[i], writes into d_out ((6, n),
+ * row k at d_out + k n): 0 the fit's erf(x) (from exp(-x^2) at the same
+ * edge), 1 the CUDA library's erff(x), 2 the fit's exp(-x^2 / 2), 3 expf of
+ * the same, 4 the fit's 1/x, 5 the IEEE 1/x.  Enqueued on `stream`.
+ */
+gmle_status gmle_math_selftest(const float *d_x, int64_t n, float *d_out, void *stream);
+
 /* Number of fit-kernel launches this context has issued (for accounting). */
 int64_t gmle_kernel_launches(const gmle_ctx *ctx);
 
@@ -259,7 +272,7 @@ typedef struct {
 } gmle_group;
 
 /*
- * Fit a mixed batch (any mix of PSF models and box sizes 5..15) of
+ * Fit a mixed batch (any mix of PSF models and box sizes 3..16) of
  * device-resident groups, enqueued on `stream` (used as given).  The groups of
  * each (camera family, model, box) present share one persistent,
  * work-stealing launch of that model's kernel; these launches run
@@ -285,7 +298,7 @@ gmle_status gmle_fit_mixed_device(gmle_ctx *ctx, const gmle_group *groups, int32
  *
  * The call allocates nothing: no cudaMalloc, cudaFree, pinned memory, stream,
  * event or host heap, and it needs no context.  Its scratch is a static device
- * array of GMLE_NOALLOC_SCRATCH_BYTES (239,104 bytes).  The array holds the
+ * array of GMLE_NOALLOC_SCRATCH_BYTES (240,640 bytes).  The array holds the
  * persistent launches' group tables, their work-stealing tile counters and a
  * skipped-ROI counter.  It is reserved on each GPU that loads the library's
  * device code and stays there until the process exits.
@@ -308,15 +321,20 @@ gmle_status gmle_fit_mixed_device(gmle_ctx *ctx, const gmle_group *groups, int32
  * shared-memory limit.  Make that first call before any stream capture.
  *
  * Zeroing: the tile counters must be zero when each launch starts.  Every
- * call copies its tables into the scratch with one host-to-device copy on
- * `stream`, ahead of its launches, and that copy writes the counters to zero.
+ * call writes its tables into the scratch, ahead of its fit launches on
+ * `stream`, by small kernels that carry the tables in their launch
+ * parameters (one per 32 704 bytes: one for up to 95 groups); that write
+ * sets the counters to zero.  The call does not wait for the stream.
  *
  * Overlap: all calls on a device share the one scratch.  Calls whose GPU work
  * overlaps race and give undefined results, e.g. calls on different streams
- * with no event ordering them.  Calls on one stream run in order.
+ * with no event ordering them.  Calls on one stream run in order.  On the
+ * host, building a call's tables and enqueuing its launches hold one
+ * process-wide lock, so calls from several threads (and devices) are
+ * enqueued one after another; none of them waits for the GPU.
  */
 #define GMLE_NOALLOC_MAX_GROUPS 1024
-#define GMLE_NOALLOC_SCRATCH_BYTES (1536 + (8 + 224) * GMLE_NOALLOC_MAX_GROUPS)
+#define GMLE_NOALLOC_SCRATCH_BYTES (3072 + (8 + 224) * GMLE_NOALLOC_MAX_GROUPS)
 gmle_status gmle_fit_mixed_device_noalloc(const gmle_group *groups, int32_t ngroups,
                                           const float *variance, const float *gain,
                                           const float *offset, int32_t ny, int32_t nx,

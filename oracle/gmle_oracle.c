@@ -47,7 +47,7 @@
  * separate so that the checker shares no code with what it checks. */
 typedef struct {
     int32_t model;      /* 0 XYNB, 1 XYNBS, 2 XYNBSXSY, 3 AstigmaticXYZNB */
-    int32_t box;        /* ROI edge length in pixels (3..15) */
+    int32_t box;        /* ROI edge length in pixels (3..ORACLE_MAX_BOX) */
     int32_t iterations; /* Newton iterations */
     int32_t camera;     /* 0 Poisson, 1 sCMOS (data in e-), 2 sCMOS (data in ADU) */
     float psf[8];
@@ -56,6 +56,10 @@ typedef struct {
     float max_step[6];
     int32_t method;     /* 0 the reference's Newton step, 1 the library's full-Hessian option */
 } oracle_desc;
+
+/* largest ROI edge the oracle takes (the reference accepts any box >= 3,
+ * src/interface.jl:22) */
+#define ORACLE_MAX_BOX 32
 
 static inline int oracle_nparams(int model)
 {
@@ -123,7 +127,7 @@ static inline double pow15d(double x) { return pow(x, 1.5); }
 static int check_desc(const oracle_desc *d)
 {
     if (d->model < 0 || d->model > 3) return -1;
-    if (d->box < 3 || d->box > 15) return -2;
+    if (d->box < 3 || d->box > ORACLE_MAX_BOX) return -2;
     if (d->iterations < 0) return -3;
     if (d->camera < 0 || d->camera > 2) return -4;
     if (d->method < 0 || d->method > 1) return -5;
@@ -171,6 +175,47 @@ int oracle_fit_f64(const oracle_desc *d, const float *data, const int32_t *xc, c
     for (int64_t r = 0; r < n; r++)
         fit_one_f64(d, data + b2 * r, xc ? xc[r] : 1, yc ? yc[r] : 1, var, gain, offset, ny,
                     params + P * r, crlb + P * r, llr + r, flags + r);
+    return 0;
+}
+
+/* The final pass (LLR, Fisher, CRLB) of n ROIs at given parameters theta
+ * ((n, P) row-major doubles, e.g. another implementation's fitted values):
+ * separates the error of a Fisher accumulation and inversion from that of the
+ * Newton iterations that led to theta. */
+int oracle_final_at_f32(const oracle_desc *d, const float *data, const int32_t *xc,
+                        const int32_t *yc, int64_t n, const float *var, const float *gain,
+                        const float *offset, int32_t ny, const double *theta, float *crlb,
+                        float *llr, uint8_t *flags, int nthreads)
+{
+    int rc = check_desc(d);
+    if (rc) return rc;
+    const int P = oracle_nparams(d->model);
+    const int64_t b2 = (int64_t)d->box * d->box;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
+#endif
+    for (int64_t r = 0; r < n; r++)
+        final_at_f32(d, data + b2 * r, xc ? xc[r] : 1, yc ? yc[r] : 1, var, gain, offset, ny,
+                     theta + P * r, crlb + P * r, llr + r, flags + r);
+    return 0;
+}
+int oracle_final_at_f64(const oracle_desc *d, const float *data, const int32_t *xc,
+                        const int32_t *yc, int64_t n, const float *var, const float *gain,
+                        const float *offset, int32_t ny, const double *theta, double *crlb,
+                        double *llr, uint8_t *flags, int nthreads)
+{
+    int rc = check_desc(d);
+    if (rc) return rc;
+    const int P = oracle_nparams(d->model);
+    const int64_t b2 = (int64_t)d->box * d->box;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
+#endif
+    for (int64_t r = 0; r < n; r++)
+        final_at_f64(d, data + b2 * r, xc ? xc[r] : 1, yc ? yc[r] : 1, var, gain, offset, ny,
+                     theta + P * r, crlb + P * r, llr + r, flags + r);
     return 0;
 }
 

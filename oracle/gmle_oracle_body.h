@@ -365,17 +365,15 @@ static int FN(crlb_from_fisher)(R *F, int n, R *crlb)
 
 /* ---- the per-ROI fit: unified_gaussian_mle_kernel!, src/unified_kernel.jl:285-434 */
 
-static void FN(fit_one)(const oracle_desc *d, const float *roi_in, int32_t xc, int32_t yc,
-                        const float *var, const float *gain, const float *offset, int32_t ny,
-                        R *out_params, R *out_crlb, R *out_llr, uint8_t *out_flags)
+/* sCMOS preprocessing, src/camera_models.jl:110-113 (to_electrons) and the
+ * camera-coordinate map lookup of src/unified_kernel.jl:277-282: the ROI's
+ * pixels in e- and its variance tile. */
+static void FN(stage_roi)(const oracle_desc *d, const float *roi_in, int32_t xc, int32_t yc,
+                          const float *var, const float *gain, const float *offset, int32_t ny,
+                          R *roi, R *vroi)
 {
-    const int box = d->box, P = oracle_nparams(d->model);
+    const int box = d->box;
     const int scmos = d->camera != 0;
-    R roi[15 * 15], vroi[15 * 15], psf[8], lo[6], hi[6], ms[6];
-    for (int t = 0; t < 8; t++) psf[t] = (R)d->psf[t];
-    for (int k = 0; k < P; k++) { lo[k] = d->lower[k]; hi[k] = d->upper[k]; ms[k] = d->max_step[k]; }
-    /* sCMOS preprocessing, src/camera_models.jl:110-113 (to_electrons) and the
-     * camera-coordinate map lookup of src/unified_kernel.jl:277-282 */
     for (int j = 1; j <= box; j++)
         for (int i = 1; i <= box; i++) {
             int p = (i - 1) + box * (j - 1);
@@ -389,6 +387,61 @@ static void FN(fit_one)(const oracle_desc *d, const float *roi_in, int32_t xc, i
             roi[p] = v;
             vroi[p] = mv;
         }
+}
+
+/* final pass: LLR + Fisher + CRLB at theta, src/unified_kernel.jl:354-431 */
+static int FN(final_pass)(const oracle_desc *d, const R *roi, const R *vroi, const R *th,
+                          const R *psf, R *out_crlb, R *out_llr)
+{
+    const int box = d->box, P = oracle_nparams(d->model);
+    const int scmos = d->camera != 0;
+    R llr = 0, F[36];
+    for (int t = 0; t < P * P; t++) F[t] = 0;
+    for (int j = 1; j <= box; j++)
+        for (int i = 1; i <= box; i++) {
+            int p = (i - 1) + box * (j - 1);
+            R mu, du[6], d2[6];
+            FN(pixel_derivatives)(d->model, i, j, th, psf, &mu, du, d2);
+            llr += FN(log_likelihood_term)(scmos, roi[p], mu, vroi[p]);
+            if (mu > 0) {
+                R v = scmos ? mu + vroi[p] : mu;
+                for (int k = 0; k < P; k++)
+                    for (int l = k; l < P; l++) {
+                        R f = du[k] * du[l] / v;
+                        F[k + P * l] += f;
+                        if (k != l) F[l + P * k] += f;
+                    }
+            }
+        }
+    *out_llr = llr;
+    return FN(crlb_from_fisher)(F, P, out_crlb);
+}
+
+/* The final pass alone at a given theta (the fitted parameters of another
+ * implementation), for the error of its Fisher accumulation and inversion. */
+static void FN(final_at)(const oracle_desc *d, const float *roi_in, int32_t xc, int32_t yc,
+                         const float *var, const float *gain, const float *offset, int32_t ny,
+                         const double *theta, R *out_crlb, R *out_llr, uint8_t *out_flags)
+{
+    const int P = oracle_nparams(d->model);
+    R roi[ORACLE_MAX_BOX * ORACLE_MAX_BOX], vroi[ORACLE_MAX_BOX * ORACLE_MAX_BOX], psf[8], th[6];
+    for (int t = 0; t < 8; t++) psf[t] = (R)d->psf[t];
+    for (int k = 0; k < P; k++) th[k] = (R)theta[k];
+    FN(stage_roi)(d, roi_in, xc, yc, var, gain, offset, ny, roi, vroi);
+    *out_flags = (uint8_t)FN(final_pass)(d, roi, vroi, th, psf, out_crlb, out_llr);
+}
+
+static void FN(fit_one)(const oracle_desc *d, const float *roi_in, int32_t xc, int32_t yc,
+                        const float *var, const float *gain, const float *offset, int32_t ny,
+                        R *out_params, R *out_crlb, R *out_llr, uint8_t *out_flags)
+{
+    const int box = d->box, P = oracle_nparams(d->model);
+    const int scmos = d->camera != 0;
+    R roi[ORACLE_MAX_BOX * ORACLE_MAX_BOX], vroi[ORACLE_MAX_BOX * ORACLE_MAX_BOX];
+    R psf[8], lo[6], hi[6], ms[6];
+    for (int t = 0; t < 8; t++) psf[t] = (R)d->psf[t];
+    for (int k = 0; k < P; k++) { lo[k] = d->lower[k]; hi[k] = d->upper[k]; ms[k] = d->max_step[k]; }
+    FN(stage_roi)(d, roi_in, xc, yc, var, gain, offset, ny, roi, vroi);
 
     R th[6];
     FN(initialize)(d->model, box, roi, psf, th);
@@ -479,26 +532,8 @@ static void FN(fit_one)(const oracle_desc *d, const float *roi_in, int32_t xc, i
     }
 
     /* final pass: LLR + Fisher, src/unified_kernel.jl:354-397 */
-    R llr = 0, F[36];
-    for (int t = 0; t < P * P; t++) F[t] = 0;
-    for (int j = 1; j <= box; j++)
-        for (int i = 1; i <= box; i++) {
-            int p = (i - 1) + box * (j - 1);
-            R mu, du[6], d2[6];
-            FN(pixel_derivatives)(d->model, i, j, th, psf, &mu, du, d2);
-            llr += FN(log_likelihood_term)(scmos, roi[p], mu, vroi[p]);
-            if (mu > 0) {
-                R v = scmos ? mu + vroi[p] : mu;
-                for (int k = 0; k < P; k++)
-                    for (int l = k; l < P; l++) {
-                        R f = du[k] * du[l] / v;
-                        F[k + P * l] += f;
-                        if (k != l) F[l + P * k] += f;
-                    }
-            }
-        }
-    R crlb[6];
-    int flags = FN(crlb_from_fisher)(F, P, crlb);
+    R llr, crlb[6];
+    int flags = FN(final_pass)(d, roi, vroi, th, psf, crlb, &llr);
     for (int k = 0; k < P; k++) { out_params[k] = th[k]; out_crlb[k] = crlb[k]; }
     *out_llr = llr;
     *out_flags = (uint8_t)flags;

@@ -50,6 +50,11 @@ def lib() -> C.CDLL:
             f.argtypes = [C.POINTER(OracleDesc), vp, vp, vp, i64, vp, vp, vp, C.c_int32,
                           C.c_int32, vp, vp, vp, vp, C.c_int]
             f.restype = C.c_int
+        for nm in ("oracle_final_at_f32", "oracle_final_at_f64"):
+            f = getattr(L, nm)
+            f.argtypes = [C.POINTER(OracleDesc), vp, vp, vp, i64, vp, vp, vp, C.c_int32,
+                          vp, vp, vp, vp, C.c_int]
+            f.restype = C.c_int
         for nm in ("oracle_crlb_at_f32", "oracle_crlb_at_f64"):
             f = getattr(L, nm)
             f.argtypes = [C.c_int, C.c_int, vp, vp, vp]
@@ -108,6 +113,37 @@ def fit(desc: OracleDesc, data: np.ndarray, xc=None, yc=None, maps=None,
     if rc != 0:
         raise ValueError(f"oracle rejected the descriptor (code {rc})")
     return {"params": params, "crlb": crlb, "llr": llr, "flags": flags}
+
+
+def final_at(desc: OracleDesc, data: np.ndarray, theta: np.ndarray, xc=None, yc=None,
+             maps=None, precision: str = "f64", threads: int = 0) -> dict:
+    """The reference's final pass (LLR, Fisher matrix, CRLB; src/unified_kernel.jl:354-431)
+    of each ROI at the given parameters theta (n, P), without the Newton
+    iterations: the error of another implementation's CRLB against this one,
+    at that implementation's own theta, is the error of its Fisher
+    accumulation and inversion alone.  Returns crlb (n, P), llr (n,), flags (n,)."""
+    L = lib()
+    data = np.asfortranarray(data, np.float32)
+    n = data.shape[2]
+    P = nparams(desc.model)
+    th = np.ascontiguousarray(theta, np.float64).reshape(n, P)
+    dt = np.float32 if precision == "f32" else np.float64
+    crlb = np.empty((n, P), dt)
+    llr = np.empty(n, dt)
+    flags = np.empty(n, np.uint8)
+    var = gain = off = None
+    ny = 0
+    if maps is not None:
+        var, gain, off = (np.asfortranarray(m, np.float32) for m in maps)
+        ny = var.shape[0]
+    xc = None if xc is None else np.ascontiguousarray(xc, np.int32)
+    yc = None if yc is None else np.ascontiguousarray(yc, np.int32)
+    f = L.oracle_final_at_f32 if precision == "f32" else L.oracle_final_at_f64
+    rc = f(C.byref(desc), _p(data), _p(xc), _p(yc), n, _p(var), _p(gain), _p(off), ny,
+           _p(th), _p(crlb), _p(llr), _p(flags), threads)
+    if rc != 0:
+        raise ValueError(f"oracle rejected the descriptor (code {rc})")
+    return {"crlb": crlb, "llr": llr, "flags": flags}
 
 
 def crlb_at(model: int, box: int, psf, theta, precision: str = "f64"):

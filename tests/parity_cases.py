@@ -8,12 +8,10 @@ from gaussmle_gb300.models import (AstigmaticXYZNB, GaussianXYNB, GaussianXYNBS,
                                    GaussianXYNBSXSY)
 from gaussmle_gb300.constraints import default_constraints
 
-# Tolerances of the parity bar: positions, sigmas and z within 1e-3 (pixels, or
-# the units of gamma and d for z), N and bg within 1e-4 relative, CRLB within
-# 1e-3 relative, identical convergence flags.
-TOL_POS = 1e-3
-TOL_REL_NBG = 1e-4
-TOL_REL_CRLB = 1e-3
+# The parity bar and the comparison live with the oracle (oracle/parity.py):
+# positions, sigmas and z within 1e-3, N and bg within 1e-4 relative, CRLB
+# within 1e-3 relative, identical convergence flags.
+from oracle.parity import TOL_POS, TOL_REL_CRLB, TOL_REL_NBG, compare  # noqa: E402,F401
 
 CASES = [
     # name, model, box, camera, n
@@ -72,21 +70,3 @@ def oracle_desc(O, w, iterations=20):
     c = w.constraints
     return O.make_desc(w.psf.model_id, w.box, iterations, w.camera, w.psf.psf_vector(),
                        c.lower, c.upper, c.max_step)
-
-
-def compare(model, got_params, got_crlb, got_flags, ref):
-    """Per-ROI pass mask and max errors against the oracle outputs."""
-    rp, rc = ref["params"].astype(np.float64), ref["crlb"].astype(np.float64)
-    gp, gc = got_params.astype(np.float64), got_crlb.astype(np.float64)
-    ipos = {0: [0, 1], 1: [0, 1, 4], 2: [0, 1, 4, 5], 3: [0, 1, 2]}[model]
-    inb = {0: [2, 3], 1: [2, 3], 2: [2, 3], 3: [3, 4]}[model]
-    dpos = np.abs(gp[:, ipos] - rp[:, ipos]).max(1)
-    dnb = (np.abs(gp[:, inb] - rp[:, inb]) / np.maximum(np.abs(rp[:, inb]), 1e-30)).max(1)
-    fin = np.isfinite(rc) & np.isfinite(gc)
-    dcr = np.where(fin, np.abs(gc - rc) / np.maximum(np.abs(rc), 1e-30), 0.0)
-    dcr = np.where(np.isfinite(rc) == np.isfinite(gc), dcr, np.inf).max(1)
-    same_flag = (got_flags & 1) == (ref["flags"] & 1)
-    ok = (dpos <= TOL_POS) & (dnb <= TOL_REL_NBG) & (dcr <= TOL_REL_CRLB) & same_flag
-    return ok, {"max_dpos": float(dpos.max()), "max_rel_nbg": float(dnb.max()),
-                "max_rel_crlb": float(dcr.max()), "flag_mismatch": int((~same_flag).sum()),
-                "pass_frac": float(ok.mean())}

@@ -1,0 +1,109 @@
+"""Every square ROI of at least 3 pixels (src/interface.jl:22), on the GPU.
+
+Boxes 3..16 run in kernels specialised for the box (one thread per ROI, or
+4 lanes per ROI); 17..64 in the run-time-box kernel.  Each case is compared
+with the FP32 oracle at the parity bar, and both with the FP64 oracle:
+  * >= 99.5 % within the bar where the FP32 path stays within the bar of the
+    FP64 iteration (the well-posed cases), else no fewer than the FP32
+    path's own fraction less 2 %;
+  * the GPU within the bar of the FP64 iteration on as many ROIs as the FP32
+    path, to 1 % of the ROIs;
+  * the same convergence flags.
+Mixed batches and serving take boxes 3..16 in one submission.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from gaussmle_gb300 import serve
+from oracle import oracle as O
+from oracle import parity
+from parity_cases import make_case, oracle_desc
+from test_parity_gpu import run_gpu
+
+pytestmark = pytest.mark.gpu
+
+CASES = [  # model, box, camera
+    (0, 3, 0), (0, 4, 0), (0, 6, 0), (0, 8, 0), (0, 10, 0), (0, 12, 0), (0, 14, 0), (0, 16, 0),
+    (0, 17, 0), (0, 24, 0), (0, 32, 2), (1, 8, 2), (1, 16, 2), (1, 20, 2), (2, 10, 0), (2, 18, 0),
+    (2, 12, 1), (3, 12, 0), (3, 16, 2), (3, 21, 2), (0, 64, 0),
+]
+
+
+def check(w, params, crlb, flags):
+    d = oracle_desc(O, w)
+    f32 = O.fit(d, w.data, w.x_corners, w.y_corners, w.maps, "f32")
+    f64 = O.fit(d, w.data, w.x_corners, w.y_corners, w.maps, "f64")
+    ok, st = parity.compare(w.psf.model_id, params, crlb, flags, f32)
+    g_in = (parity.distance(w.psf.model_id, params, f64["params"]) <= 1).mean()
+    f_in = (parity.distance(w.psf.model_id, f32["params"], f64["params"]) <= 1).mean()
+    print(f"\n{w.name}: {st}; within the bar of FP64: GPU {g_in:.3f}, FP32 {f_in:.3f}")
+    assert st["pass_frac"] >= (0.995 if f_in >= 0.999 else f_in - 0.02), st
+    assert g_in >= f_in - 0.01, (g_in, f_in)
+    assert st["flag_mismatch"] == 0, st
+
+
+@pytest.mark.parametrize("model,box,camera", CASES,
+                         ids=[f"m{m}-box{b}-cam{c}" for m, b, c in CASES])
+def test_every_box_matches_the_oracle(ctx, model, box, camera):
+    n = 200 if box > 32 else 600
+    w = make_case(f"m{model}-{box}-{camera}", model, box, camera, n, sensor=256)
+    params, crlb, llr, flags = run_gpu(ctx, w)
+    check(w, params, crlb, flags)
+
+
+@pytest.mark.parametrize("tpr,rpb", [(1, 32), (1, 128), (4, 32), (4, 64)])
+@pytest.mark.parametrize("model,box,camera", [(0, 8, 0), (1, 16, 2), (3, 6, 0), (2, 14, 2)])
+def test_new_boxes_every_launch_shape(ctx, model, box, camera, tpr, rpb):
+    w = make_case(f"m{model}-{box}-{camera}", model, box, camera, 500)
+    ctx.check(ctx.lib.gmle_set_tuning(ctx.handle, model, box, camera, tpr, rpb))
+    try:
+        params, crlb, llr, flags = run_gpu(ctx, w)
+    finally:
+        ctx.check(ctx.lib.gmle_set_tuning(ctx.handle, model, box, camera, 0, 0))
+    check(w, params, crlb, flags)
+
+
+def test_eight_lanes_are_for_odd_boxes_only(ctx):
+    assert ctx.lib.gmle_set_tuning(ctx.handle, 0, 8, 0, 8, 16) == 1  # GMLE_INVALID_ARG
+    assert ctx.lib.gmle_set_tuning(ctx.handle, 0, 9, 0, 8, 16) == 0
+    ctx.check(ctx.lib.gmle_set_tuning(ctx.handle, 0, 9, 0, 0, 0))
+
+
+def test_boxes_beyond_64_and_below_3_are_rejected(ctx):
+    w = make_case("xynb-11-poisson", 0, 11, 0, 4)
+    from gaussmle_gb300.fitter import make_desc
+    for box in (2, 65):
+        desc = make_desc(w.psf, box, 20, w.constraints, 0)
+        z = np.zeros(box * box * 4, np.float32)
+        out = np.zeros(64, np.float32)
+        p = lambda a: a.ctypes.data_as(C.c_void_p)
+        st = ctx.lib.gmle_fit(ctx.handle, C.byref(desc), p(z), None, None, 4, p(out), p(out),
+                              p(out), None)
+        assert st == 3, box  # GMLE_UNSUPPORTED_BOX
+
+
+def test_mixed_batch_with_new_boxes_matches_plain_fits(ctx):
+    """One gmle_fit_mixed_device submission over boxes 4, 8, 12 and 16 (table
+    launches) gives the same results as plain per-group fits."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda", 0)
+    ws = [make_case(f"m{m}-{b}", m, b, 0, 700, seed=900 + b) for m, b in
+          [(0, 4), (0, 8), (1, 12), (3, 16)]]
+    groups, outs = [], []
+    for w in ws:
+        n, P = w.n, w.psf.nparams
+        data = torch.from_numpy(np.ascontiguousarray(w.data.transpose(2, 1, 0)).reshape(-1)).to(dev)
+        o = {"params": torch.empty((n, P), device=dev), "crlb": torch.empty((n, P), device=dev),
+             "llr": torch.empty(n, device=dev), "flags": torch.empty(n, dtype=torch.uint8,
+                                                                      device=dev), "data": data}
+        outs.append(o)
+        groups.append(serve.make_group(w.psf, w.box, 0, w.constraints, data, None, None,
+                                       o["params"], o["crlb"], o["llr"], o["flags"]))
+    serve.fit_mixed_device(ctx, groups)
+    torch.cuda.synchronize()
+    for w, o in zip(ws, outs):
+        params, crlb, llr, flags = run_gpu(ctx, w)
+        assert np.array_equal(o["params"].cpu().numpy(), params), w.name
+        assert np.array_equal(o["flags"].cpu().numpy(), flags), w.name

@@ -64,7 +64,7 @@ def _dev(torch, w):
 
 # Launch shapes forced per kind so that the table launch and the plain launch
 # run the same code: both kernels (one and several threads per ROI) are covered.
-SHAPES = [(1, 32), (2, 64), (4, 32), (1, 64), (8, 16)]
+SHAPES = [(1, 32), (4, 64), (4, 32), (1, 64), (8, 16)]
 
 
 def test_mixed_launch_matches_plain_kernel(ctx):

@@ -12,6 +12,7 @@ import pytest
 import gaussmle_gb300 as G
 from gaussmle_gb300.fitter import make_desc
 from oracle import oracle as O
+from oracle import parity
 from parity_cases import CASES, compare, make_case, oracle_desc
 
 pytestmark = pytest.mark.gpu
@@ -19,7 +20,10 @@ pytestmark = pytest.mark.gpu
 # Fraction of ROIs that must meet every tolerance.  Fixed-iteration clamped
 # Newton is discontinuous at the clamps: ulp-level differences (erf/exp
 # implementations, FMA contraction, summation order) can flip a clamp for a
-# fit that has not converged, so a small fraction may differ.
+# fit that has not converged, so a small fraction may differ.  On the
+# astigmatic cases the FP32 reference path itself is off the FP64 iteration
+# by more than the bar on about 1 ROI in 50; the test checks below that the
+# GPU is as close to the FP64 iteration as the FP32 path is.
 MIN_PASS = {"astig-15-poisson": 0.97, "astig-15-scmos-adu": 0.97}
 DEFAULT_MIN_PASS = 0.995
 
@@ -54,11 +58,19 @@ def test_parity_vs_oracle(ctx, case):
     ok, st = compare(w.psf.model_id, params, crlb, flags, ref)
     llr_rel = np.abs(llr - ref["llr"]) / np.maximum(np.abs(ref["llr"]), 1e-6)
     st["llr_rel_p99"] = float(np.quantile(llr_rel, 0.99))
-    # error of each against the FP64 oracle (stated, checked loosely)
+    # error of each against the FP64 oracle of the same iteration
     e_gpu = np.abs(params - ref64["params"]).max(0)
     e_f32 = np.abs(ref["params"] - ref64["params"]).max(0)
-    print(f"\n{w.name}: {st}\n  max|GPU-FP64| {e_gpu}\n  max|F32-FP64| {e_f32}")
+    d_gpu = parity.distance(w.psf.model_id, params, ref64["params"])
+    d_f32 = parity.distance(w.psf.model_id, ref["params"], ref64["params"])
+    print(f"\n{w.name}: {st}\n  max|GPU-FP64| {e_gpu}\n  max|F32-FP64| {e_f32}"
+          f"\n  within the bar of FP64: GPU {(d_gpu <= 1).mean():.4f}, "
+          f"FP32 {(d_f32 <= 1).mean():.4f}")
     assert st["pass_frac"] >= MIN_PASS.get(w.name, DEFAULT_MIN_PASS), st
+    # the GPU is as close to the exact (FP64) iteration as the FP32 reference
+    # path is, to 1 % of the ROIs: the misses of the astigmatic cases are the
+    # iteration's own sensitivity, shared by the FP32 path
+    assert (d_gpu <= 1).mean() >= (d_f32 <= 1).mean() - 0.01
     assert np.quantile(llr_rel, 0.99) < 1e-4
 
 
@@ -87,10 +99,11 @@ SHAPE_CASES = [c for c in CASES if c[0] in ("xynb-11-poisson", "xynbs-13-scmos-a
                                            "xynbsxsy-13-scmos-adu", "astig-15-poisson")]
 
 
-@pytest.mark.parametrize("tpr,rpb", [(1, 32), (1, 64), (2, 32), (4, 32), (8, 16)])
+@pytest.mark.parametrize("tpr,rpb", [(1, 32), (1, 64), (1, 128), (4, 32), (4, 64), (8, 16),
+                                     (8, 32)])
 @pytest.mark.parametrize("case", SHAPE_CASES, ids=[c[0] for c in SHAPE_CASES])
 def test_parity_every_launch_shape(ctx, case, tpr, rpb):
-    """Both kernels (one thread per ROI, and lane groups of 2..8) meet the bar."""
+    """Both kernels (one thread per ROI, and lane groups of 4 and 8) meet the bar."""
     name, model, box, camera, n = case
     w = make_case(name, model, box, camera, min(n, 1500))
     ctx.check(ctx.lib.gmle_set_tuning(ctx.handle, model, box, camera, tpr, rpb))

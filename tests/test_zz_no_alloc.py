@@ -105,9 +105,9 @@ def test_invalid_groups_are_rejected_with_a_message():
     err = C.create_string_buffer(256)
     st = lib.gmle_fit_mixed_device_noalloc(C.byref(g), 1, None, None, None, 0, 0, None, err, 256)
     assert st == 1 and b"variance" in err.value  # an sCMOS group with no maps
-    g.desc.box = 8
-    st = lib.gmle_fit_mixed_device_noalloc(C.byref(g), 1, None, None, None, 0, 0, None, None, 0)
-    assert st == 3  # GMLE_UNSUPPORTED_BOX
+    g.desc.box = 17  # boxes above 16 run through gmle_fit / gmle_fit_device only
+    st = lib.gmle_fit_mixed_device_noalloc(C.byref(g), 1, None, None, None, 0, 0, None, err, 256)
+    assert st == 3 and b"3..16" in err.value  # GMLE_UNSUPPORTED_BOX
 
 
 @pytest.mark.gpu
@@ -154,3 +154,79 @@ def test_noalloc_matches_the_context_entry_point_on_two_calls(ctx):
             assert np.array_equal(got["flags"], want["flags"]), (call, w.name)
             np.testing.assert_allclose(got["llr"], want["llr"], rtol=1e-4, atol=1e-3,
                                        err_msg=f"call {call} {w.name}")
+
+
+@pytest.mark.gpu
+def test_noalloc_many_small_groups_of_two_kinds(ctx):
+    """1024 groups (the static table's limit) of 1..300 ROIs of two kinds, most
+    of them not a whole number of blocks: each group's tile lookup (a binary
+    search over the groups' first tiles) and the arguments at the end of the
+    static table, against gmle_fit_mixed_device group by group."""
+    torch = pytest.importorskip("torch")
+    lib = _lib_loaded()
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(11)
+    maps = simulate.scmos_maps(np.random.Generator(np.random.Philox(78)), SENSOR, SENSOR)
+    var, gain, off = (np.asfortranarray(m, np.float32) for m in maps)
+    ctx.check(ctx.lib.gmle_set_calibration(ctx.handle, var.ctypes.data_as(C.c_void_p),
+                                           gain.ctypes.data_as(C.c_void_p),
+                                           off.ctypes.data_as(C.c_void_p), SENSOR, SENSOR))
+    sizes = rng.integers(1, 301, 1024)
+    kinds = rng.integers(0, 2, 1024)  # 0: XYNB 11x11 Poisson, 1: XYNBS 9x9 sCMOS ADU
+    base = []
+    for kind in (0, 1):
+        n = int(sizes[kinds == kind].sum())
+        w = make_case("xynb-11-poisson", 0, 11, 0, n, seed=500) if kind == 0 else None
+        if kind == 1:
+            w0 = make_case("xynbs-9-poisson", 1, 9, 0, n, seed=501)
+            r = np.random.Generator(np.random.Philox(502))
+            xc, yc = simulate.random_corners(r, n, 9, SENSOR, SENSOR)
+            data = simulate.scmos_rois(r, w0.psf, w0.truth, 9, maps, xc, yc)
+            w = simulate.Workload("xynbs-9-adu", w0.psf, 9, 2, w0.constraints,
+                                  np.asfortranarray(data), xc, yc, w0.truth, maps=maps)
+        base.append((w, _device_buffers(torch, [w])[0]))
+    P = [4, 5]
+    outs = [[{"params": torch.full((int(sizes[kinds == k].sum()), P[k]), float("nan"), device=dev),
+              "crlb": torch.full((int(sizes[kinds == k].sum()), P[k]), float("nan"), device=dev),
+              "llr": torch.full((int(sizes[kinds == k].sum()),), float("nan"), device=dev),
+              "flags": torch.zeros(int(sizes[kinds == k].sum()), dtype=torch.uint8, device=dev)}
+             for k in (0, 1)] for _ in range(2)]
+
+    def table(o):
+        gs, lo = [], [0, 0]
+        for n, k in zip(sizes, kinds):
+            w, i = base[k]
+            a, b2 = lo[k], w.box * w.box
+            g = serve.make_group(w.psf, w.box, w.camera, w.constraints, i["data"], i["xc"],
+                                 i["yc"], o[k]["params"], o[k]["crlb"], o[k]["llr"],
+                                 o[k]["flags"])
+            g.data = C.c_void_p(i["data"].data_ptr() + 4 * a * b2)
+            g.x_corners = C.c_void_p(i["xc"].data_ptr() + 4 * a)
+            g.y_corners = C.c_void_p(i["yc"].data_ptr() + 4 * a)
+            g.n = int(n)
+            g.params = C.c_void_p(o[k]["params"].data_ptr() + 4 * a * P[k])
+            g.crlb = C.c_void_p(o[k]["crlb"].data_ptr() + 4 * a * P[k])
+            g.llr = C.c_void_p(o[k]["llr"].data_ptr() + 4 * a)
+            g.flags = C.c_void_p(o[k]["flags"].data_ptr() + a)
+            gs.append(g)
+            lo[k] += int(n)
+        return (_lib.Group * len(gs))(*gs)
+
+    stream = torch.cuda.Stream()
+    ctx.check(ctx.lib.gmle_fit_mixed_device(ctx.handle, table(outs[0]), 1024,
+                                            C.c_void_p(stream.cuda_stream)))
+    d_maps = [torch.from_numpy(np.ascontiguousarray(m.T)).to(dev) for m in (var, gain, off)]
+    err = C.create_string_buffer(512)
+    st = lib.gmle_fit_mixed_device_noalloc(table(outs[1]), 1024,
+                                           *(C.c_void_p(m.data_ptr()) for m in d_maps),
+                                           SENSOR, SENSOR, C.c_void_p(stream.cuda_stream), err, 512)
+    assert st == 0, err.value
+    stream.synchronize()
+    for k in (0, 1):
+        w = base[k][0]
+        got = {key: v.cpu().numpy() for key, v in outs[1][k].items()}
+        want = {key: v.cpu().numpy() for key, v in outs[0][k].items()}
+        assert not np.isnan(got["params"]).any(), f"kind {k}: ROIs left unfitted"
+        ok, s = compare(w.psf.model_id, got["params"], got["crlb"], got["flags"], want)
+        assert s["pass_frac"] == 1.0, (k, s)
+        assert np.array_equal(got["flags"], want["flags"]), k
