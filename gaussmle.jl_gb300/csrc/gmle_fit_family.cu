@@ -8,14 +8,6 @@
 #error "compile with -DGMLE_MODEL=<0..3> -DGMLE_SCMOS=<0|1> -DGMLE_PART=<0..2>"
 #endif
 
-#if GMLE_PART == 0
-#define GMLE_PART_BOXES GMLE_CASE_PART0
-#elif GMLE_PART == 1
-#define GMLE_PART_BOXES GMLE_CASE_PART1
-#else
-#define GMLE_PART_BOXES GMLE_CASE_PART2
-#endif
-
 #include "gmle_launch.cuh"
 
 namespace gmle {

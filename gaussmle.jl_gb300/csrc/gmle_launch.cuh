@@ -121,21 +121,22 @@ inline size_t launch_smem(int model, int box, bool scmos, int tpr, int rpb, bool
 
 using FitKernel = void (*)(const KernelArgs, const TileTable);
 
-// The kernels of a part: defined where GMLE_PART (and GMLE_PART_BOXES) are,
-// in gmle_fit_family.cu.
-#ifdef GMLE_PART
-template <int MODEL, int BOX, bool SCMOS>
+// The kernels of a part.  PART is a template parameter (not the GMLE_PART
+// macro of the unit that compiles them) so that the instantiations of two
+// parts never share a name: template instantiations of the same name are
+// merged at link time.  They are instantiated in gmle_fit_family.cu only.
+template <int MODEL, int BOX, bool SCMOS, int PART>
 cudaError_t kernel_for(int tpr, bool table, bool lm, FitKernel *kern)
 {
-    constexpr int PART = part_of(BOX, 1) == 0 ? 0 : 1;  // this box's one-thread part
+    constexpr int R1PART = part_of(BOX, 1);  // this box's one-thread part
     const bool r1 = tpr == 1;
     if (lm && (!r1 || table)) return cudaErrorInvalidConfiguration;
     if (!tpr_supported(tpr, BOX)) return cudaErrorInvalidConfiguration;
-    if constexpr (GMLE_PART == PART) {
+    if constexpr (PART == R1PART) {
         if (!r1) return cudaErrorInvalidConfiguration;
         if (lm) *kern = fit_kernel_r1<MODEL, BOX, SCMOS, false, true>;
         else *kern = table ? fit_kernel_r1<MODEL, BOX, SCMOS, true> : fit_kernel_r1<MODEL, BOX, SCMOS, false>;
-    } else if constexpr (GMLE_PART == 2) {
+    } else if constexpr (PART == 2) {
         if (r1) return cudaErrorInvalidConfiguration;
         if (tpr == 4) *kern = table ? fit_kernel<MODEL, BOX, SCMOS, true, 4> : fit_kernel<MODEL, BOX, SCMOS, false, 4>;
         else if constexpr (main_box(BOX))
@@ -163,7 +164,7 @@ cudaError_t kernel_for(int tpr, bool table, bool lm, FitKernel *kern)
     return e;
 }
 
-template <int MODEL, int BOX, bool SCMOS>
+template <int MODEL, int BOX, bool SCMOS, int PART>
 cudaError_t launch_one(const KernelArgs &a, const TileTable &t, const LaunchShape &shape,
                        cudaStream_t s)
 {
@@ -174,7 +175,7 @@ cudaError_t launch_one(const KernelArgs &a, const TileTable &t, const LaunchShap
     if (tpr == 1 && threads > kMaxThreadsR1) return cudaErrorInvalidConfiguration;
     const size_t smem = launch_smem(MODEL, BOX, SCMOS, tpr, rpb, table);
     FitKernel kern;
-    cudaError_t e = kernel_for<MODEL, BOX, SCMOS>(tpr, table, shape.lm, &kern);
+    cudaError_t e = kernel_for<MODEL, BOX, SCMOS, PART>(tpr, table, shape.lm, &kern);
     if (e != cudaSuccess) return e;
     const int64_t blocks = table ? shape.grid : (a.n + rpb - 1) / rpb;
     if (blocks <= 0) return cudaSuccess;
@@ -212,11 +213,11 @@ inline int tmem_kernel_blocks_per_sm(FitKernel kern, int threads, size_t dyn_sme
     return std::max(0, std::min({by_regs, by_smem, by_threads, blk_sm, by_tmem}));
 }
 
-template <int MODEL, int BOX, bool SCMOS>
+template <int MODEL, int BOX, bool SCMOS, int PART>
 int table_blocks_one(int tpr, int rpb)
 {
     FitKernel kern;
-    cudaError_t e = kernel_for<MODEL, BOX, SCMOS>(tpr, true, false, &kern);
+    cudaError_t e = kernel_for<MODEL, BOX, SCMOS, PART>(tpr, true, false, &kern);
     if (e != cudaSuccess) return -(int)e;
     const size_t smem = launch_smem(MODEL, BOX, SCMOS, tpr, rpb, true);
     int nb = 0;
@@ -235,15 +236,23 @@ int table_blocks_one(int tpr, int rpb)
 #define GMLE_CASE_PART1(CALL) CALL(3) CALL(4) CALL(6) CALL(8) CALL(10) CALL(12) CALL(14) CALL(16)
 #define GMLE_CASE_PART2(CALL) GMLE_CASE_PART0(CALL) GMLE_CASE_PART1(CALL)
 
+// A part's boxes: odd 5..15 (part 0), the other boxes 3..16 (part 1), all
+// boxes 3..16 (part 2).
+#define GMLE_PART_SWITCH(GMLE_CASE)                                 \
+    if constexpr (PART == 0) {                                      \
+        switch (box) { GMLE_CASE_PART0(GMLE_CASE) default: break; } \
+    } else if constexpr (PART == 1) {                               \
+        switch (box) { GMLE_CASE_PART1(GMLE_CASE) default: break; } \
+    } else {                                                        \
+        switch (box) { GMLE_CASE_PART2(GMLE_CASE) default: break; } \
+    }
+
 template <int MODEL, bool SCMOS, int PART>
 cudaError_t launch_part(int box, const KernelArgs &a, const TileTable &t, const LaunchShape &shape,
                         cudaStream_t s)
 {
-#define GMLE_CASE(B) case B: return launch_one<MODEL, B, SCMOS>(a, t, shape, s);
-    switch (box) {
-        GMLE_PART_BOXES(GMLE_CASE)
-        default: break;
-    }
+#define GMLE_CASE(B) case B: return launch_one<MODEL, B, SCMOS, PART>(a, t, shape, s);
+    GMLE_PART_SWITCH(GMLE_CASE)
 #undef GMLE_CASE
     return cudaErrorInvalidValue;
 }
@@ -251,15 +260,12 @@ cudaError_t launch_part(int box, const KernelArgs &a, const TileTable &t, const 
 template <int MODEL, bool SCMOS, int PART>
 int table_blocks_part(int box, int tpr, int rpb)
 {
-#define GMLE_CASE(B) case B: return table_blocks_one<MODEL, B, SCMOS>(tpr, rpb);
-    switch (box) {
-        GMLE_PART_BOXES(GMLE_CASE)
-        default: break;
-    }
+#define GMLE_CASE(B) case B: return table_blocks_one<MODEL, B, SCMOS, PART>(tpr, rpb);
+    GMLE_PART_SWITCH(GMLE_CASE)
 #undef GMLE_CASE
     return 0;
 }
-#endif
+#undef GMLE_PART_SWITCH
 
 #define GMLE_EXTERN_PART(M, S, P)                                                            \
     extern template cudaError_t launch_part<M, S, P>(int, const KernelArgs &, const TileTable &, \

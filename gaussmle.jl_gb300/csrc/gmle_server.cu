@@ -24,7 +24,10 @@
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <string>
 #include <deque>
 #include <map>
 #include <thread>
@@ -67,6 +70,10 @@ struct Request {
     int64_t off = -1, bytes = 0;
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
     Clock::time_point t_submit, t_done;
+    // timeline (recorded when GMLE_SERVER_TRACE names a file): admitted (input
+    // copy issued), joined a step (its copy had landed), step launched
+    Clock::time_point t_admit, t_join, t_launch;
+    int64_t step_id = -1;
     ReqState state = PENDING;
     gmle_status status = GMLE_OK;
 };
@@ -154,6 +161,38 @@ struct Server {
     std::vector<float> lat_ms;
     Clock::time_point first_submit, last_done;
     bool have_first = false;
+    // request timeline, written to trace_path as CSV when the server stops
+    std::string trace_path;
+    struct TraceRow {
+        uint64_t ticket;
+        int64_t n, step;
+        int kind;
+        double submit, admit, join, launch, done;  // ms since the server started
+    };
+    std::vector<TraceRow> trace;
+    Clock::time_point t_start;
+
+    void trace_request(const Request *r)
+    {
+        if (trace_path.empty() || trace.size() >= (1u << 22)) return;
+        auto ms = [&](Clock::time_point t) {
+            return std::chrono::duration<double, std::milli>(t - t_start).count();
+        };
+        trace.push_back({r->ticket, r->host.n, r->step_id, kind_of(r->host.desc), ms(r->t_submit),
+                         ms(r->t_admit), ms(r->t_join), ms(r->t_launch), ms(r->t_done)});
+    }
+    void write_trace() const
+    {
+        if (trace_path.empty()) return;
+        FILE *f = std::fopen(trace_path.c_str(), "w");
+        if (!f) return;
+        std::fprintf(f, "ticket,n,kind,step,submit_ms,admit_ms,join_ms,launch_ms,done_ms\n");
+        for (const TraceRow &t : trace)
+            std::fprintf(f, "%llu,%lld,%d,%lld,%.4f,%.4f,%.4f,%.4f,%.4f\n",
+                         (unsigned long long)t.ticket, (long long)t.n, t.kind, (long long)t.step,
+                         t.submit, t.admit, t.join, t.launch, t.done);
+        std::fclose(f);
+    }
 
     cudaEvent_t get_event()
     {
@@ -220,6 +259,7 @@ struct Server {
     void complete(Request *r)
     {
         r->t_done = Clock::now();
+        trace_request(r);
         r->state = DONE;
         arena.release(r->off, r->bytes);
         r->off = -1;
@@ -367,6 +407,7 @@ struct Server {
                 r->state = STAGED;
                 lk.unlock();
                 const cudaError_t e = issue_in(r);
+                r->t_admit = Clock::now();
                 lk.lock();
                 if (e != cudaSuccess) {
                     cuda_fail(nullptr, e, "input copy");
@@ -395,6 +436,8 @@ struct Server {
                     rois += r->host.n;
                     ngroups++;
                     r->state = RUNNING;
+                    r->t_join = Clock::now();
+                    r->step_id = steps;
                     step.push_back(r);
                 }
                 staged.erase(staged.begin(), staged.begin() + taken);
@@ -403,6 +446,8 @@ struct Server {
                     std::vector<cudaEvent_t> done;
                     lk.unlock();
                     const gmle_status st = launch_step(slot, step, done);
+                    const Clock::time_point tl = Clock::now();
+                    for (Request *r : step) r->t_launch = tl;
                     lk.lock();
                     if (st != GMLE_OK) {
                         // launches already enqueued still read the slot's
@@ -486,6 +531,7 @@ void server_destroy(gmle_ctx *ctx)
     }
     S->cv_work.notify_all();
     if (S->th.joinable()) S->th.join();
+    S->write_trace();
     cudaSetDevice(ctx->device);
     for (int k = 0; k < kRunStreams; k++)
         if (S->s_run[k]) cudaStreamSynchronize(S->s_run[k]);
@@ -591,6 +637,12 @@ gmle_status gmle_server_start(gmle_ctx *ctx, const gmle_server_config *config)
         cudaEvent_t e = nullptr;
         if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess) S->event_pool.push_back(e);
     }
+    // a request timeline for diagnosis, written when the server stops
+    if (const char *tp = std::getenv("GMLE_SERVER_TRACE")) {
+        S->trace_path = tp;
+        S->trace.reserve(1 << 16);
+    }
+    S->t_start = Clock::now();
     S->th = std::thread([S] { S->loop(); });
     return GMLE_OK;
 }

@@ -7,7 +7,7 @@ arrays (data, 1-based corners, frame indices, camera).
 """
 from __future__ import annotations
 
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 
 import numpy as np
 
@@ -39,7 +39,6 @@ class SCMOSCamera:
     offset: np.ndarray | float = 0.0
     gain: np.ndarray | float = 1.0
     qe: np.ndarray | float = 1.0
-    _maps: tuple | None = field(default=None, repr=False)
 
     @property
     def pixel_edges_x(self) -> np.ndarray:
@@ -59,11 +58,10 @@ class SCMOSCamera:
 
     def calibration_maps(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
         """(variance = readnoise^2, gain, offset) as full-sensor Float32 maps
-        (extract_variance_map, src/interface.jl:43-55)."""
-        if self._maps is None:
-            rn = self._full(self.readnoise)
-            self._maps = (rn * rn, self._full(self.gain), self._full(self.offset))
-        return self._maps
+        (extract_variance_map, src/interface.jl:43-55), from the camera's
+        current arrays."""
+        rn = self._full(self.readnoise)
+        return (rn * rn, self._full(self.gain), self._full(self.offset))
 
 
 @dataclass

@@ -11,6 +11,7 @@ device: asking for one, or running without the library or a GB300, raises.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -18,6 +19,7 @@ import numpy as np
 from . import _lib
 from .camera import IdealCamera, ROIBatch, SCMOSCamera
 from .constraints import ParameterConstraints, default_constraints
+from .emitters import BasicSMLD, to_emitters
 from .models import GaussianXYNB, PSFModel
 
 
@@ -110,6 +112,7 @@ class LocalizationResult:
     frame_indices: np.ndarray
     psf_model: PSFModel
     pixel_size: float
+    camera: object = None
 
     def __len__(self) -> int:
         return self.params.shape[0]
@@ -117,22 +120,21 @@ class LocalizationResult:
     def column(self, name: str) -> np.ndarray:
         return self.params[:, self.psf_model.param_names.index(name)]
 
-    def to_smld(self) -> dict:
-        """Columnar BasicSMLD: positions and their CRLBs in microns
-        (to_emitter, src/roi_batch.jl:125-302)."""
-        px = np.float32(self.pixel_size)
-        out = {
-            "x": (self.x_camera - 1) * px, "y": (self.y_camera - 1) * px,
-            "sigma_x_err": self.uncertainties[:, 0] * px,
-            "sigma_y_err": self.uncertainties[:, 1] * px,
-            "pvalue": self.pvalues, "frame": self.frame_indices,
-        }
-        names = self.psf_model.param_names
-        for k, nm in enumerate(names[2:], start=2):
-            scale = px if nm.startswith("sigma") else np.float32(1)
-            out[nm] = self.params[:, k] * scale
-            out[nm + "_err"] = self.uncertainties[:, k] * scale
-        return out
+    def to_emitters(self, dataset: int = 1, track_id: int = 0) -> np.ndarray:
+        """Every fit as a record of the model's emitter type, in bulk
+        (to_emitter, src/roi_batch.jl:125-302; gaussmle_gb300.emitters)."""
+        cam = self.camera
+        psx = float(cam.pixel_edges_x[1] - cam.pixel_edges_x[0]) if cam else self.pixel_size
+        psy = float(cam.pixel_edges_y[1] - cam.pixel_edges_y[0]) if cam else self.pixel_size
+        return to_emitters(self.psf_model.model_id, self.params, self.uncertainties,
+                           self.pvalues, self.x_camera, self.y_camera, self.frame_indices,
+                           psx, psy, dataset, track_id)
+
+    def to_smld(self, dataset: int = 1) -> BasicSMLD:
+        """BasicSMLD of the fits (to_smld, src/roi_batch.jl:326-353)."""
+        n_frames = int(self.frame_indices.max()) if len(self.frame_indices) else 0
+        meta = {"psf_model": type(self.psf_model).__name__, "n_fits": len(self)}
+        return BasicSMLD(self.to_emitters(dataset), self.camera, n_frames, 1, meta)
 
 
 def _pvalues(ctx: _lib.Context, llr: np.ndarray, box: int, nparams: int) -> np.ndarray:
@@ -188,13 +190,36 @@ def fit(fitter: GaussMLEFitter, data, variance_map: np.ndarray | None = None):
         camera = _lib.CAMERA_SCMOS
     params, crlb, llr, flags = _run(fitter, data_f, psf_pixels, camera, xc, yc)
     pv = _pvalues(fitter.context, llr, box, psf_pixels.nparams)
+    # the reference's Array path fits on a synthetic camera of ROIs side by
+    # side, 0.1 micron pixels (src/interface.jl:191-215)
+    cam = IdealCamera(box * n, box, pixel_size)
     return LocalizationResult(params, crlb, llr, pv, flags,
                               (xc + params[:, 0] - 1).astype(np.float32),
                               (yc + params[:, 1] - 1).astype(np.float32),
-                              np.ones(n, np.int32), fitter.psf_model, pixel_size)
+                              np.ones(n, np.int32), fitter.psf_model, pixel_size, cam)
 
 
 _calibrated: dict = {}
+
+
+def ensure_calibration(ctx: _lib.Context, cam: SCMOSCamera) -> bool:
+    """Make the camera's maps the context's resident calibration; returns
+    whether they were uploaded.  The resident maps are reused while their
+    contents are unchanged: they are compared with the copy taken at upload,
+    so an in-place edit of a camera's arrays, or another camera, uploads
+    again (the reference uploads the maps with every batch,
+    src/interface.jl:431-432)."""
+    maps = [np.asfortranarray(m, np.float32) for m in cam.calibration_maps()]
+    known = _calibrated.get(id(ctx))
+    if known is not None and known[0]() is ctx and all(
+            a.shape == b.shape and np.array_equal(a, b) for a, b in zip(known[1], maps)):
+        return False
+    var, gain, off = maps
+    ctx.check(ctx.lib.gmle_set_calibration(
+        ctx.handle, var.ctypes.data_as(C.c_void_p), gain.ctypes.data_as(C.c_void_p),
+        off.ctypes.data_as(C.c_void_p), cam.ny, cam.nx))
+    _calibrated[id(ctx)] = (weakref.ref(ctx), [m.copy() for m in maps])
+    return True
 
 
 def _fit_batch(fitter: GaussMLEFitter, batch: ROIBatch):
@@ -210,14 +235,7 @@ def _fit_batch(fitter: GaussMLEFitter, batch: ROIBatch):
     if isinstance(cam, SCMOSCamera):
         # Maps are uploaded once per (context, camera) and stay resident; the
         # ADU -> e- conversion (src/camera_models.jl:110-113) runs on the device.
-        key = (id(ctx), id(cam))
-        if _calibrated.get(key) is not cam:
-            var, gain, off = (np.asfortranarray(m) for m in cam.calibration_maps())
-            ctx.check(ctx.lib.gmle_set_calibration(
-                ctx.handle, var.ctypes.data_as(C.c_void_p), gain.ctypes.data_as(C.c_void_p),
-                off.ctypes.data_as(C.c_void_p), cam.ny, cam.nx))
-            _calibrated.clear()
-            _calibrated[key] = cam
+        ensure_calibration(ctx, cam)
         camera = _lib.CAMERA_SCMOS_ADU
     elif isinstance(cam, IdealCamera):
         camera = _lib.CAMERA_POISSON
@@ -229,4 +247,4 @@ def _fit_batch(fitter: GaussMLEFitter, batch: ROIBatch):
     return LocalizationResult(params, crlb, llr, pv, flags,
                               (batch.x_corners + params[:, 0] - 1).astype(np.float32),
                               (batch.y_corners + params[:, 1] - 1).astype(np.float32),
-                              batch.frame_indices, fitter.psf_model, pixel_size)
+                              batch.frame_indices, fitter.psf_model, pixel_size, cam)

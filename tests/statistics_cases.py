@@ -24,7 +24,8 @@ import numpy as np
 
 from gaussmle_gb300 import simulate
 from gaussmle_gb300.constraints import default_constraints
-from gaussmle_gb300.models import GaussianXYNB, GaussianXYNBS, GaussianXYNBSXSY
+from gaussmle_gb300.models import (AstigmaticXYZNB, GaussianXYNB, GaussianXYNBS,
+                                   GaussianXYNBSXSY)
 
 # (bias tolerance, std/CRLB tolerance), test/validation_utils.jl:321-330
 TOL = {"x": (0.15, 0.1), "y": (0.15, 0.1), "photons": (100.0, 0.1), "bg": (2.0, 0.1),
@@ -63,6 +64,49 @@ def check_model_validation(fit, model: int, n: int = 1000, box: int = 15) -> dic
         btol, stol = TOL[name]
         out[name] = {"bias": bias, "std_ratio": ratio,
                      "pass": abs(bias) < btol and abs(1 - ratio) < stol}
+    return out
+
+
+def astig_validation_data(n: int = 1000, box: int = 15, seed: int = 42):
+    """test/validation_utils_roibatch.jl:10-58: the astigmatic calibration of
+    test/model_validation_tests.jl:97-135 (sigma0 0.13 um, Ax, Ay = +-0.05,
+    Bx, By = +-0.01, gamma 0.2 um, d 0.5 um, pixels 0.1 um: sigma0 = 1.3 px,
+    z in microns), x, y = box/2 + 0.5 randn, z U(-0.25, 0.25) um,
+    N = 2000 U(0.8, 1.2), bg = 1 U(0.8, 1.2), Poisson (IdealCamera)."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    psf = AstigmaticXYZNB(1.3, 1.3, 0.05, -0.05, 0.01, -0.01, 0.2, 0.5)
+    x = box / 2 + 0.5 * rng.standard_normal(n)
+    y = box / 2 + 0.5 * rng.standard_normal(n)
+    z = -0.25 + 0.5 * rng.uniform(0, 1, n)
+    N = 2000.0 * (0.8 + 0.4 * rng.uniform(0, 1, n))
+    bg = 1.0 * (0.8 + 0.4 * rng.uniform(0, 1, n))
+    truth = np.stack([x, y, z, N, bg], 1).astype(np.float32)
+    return psf, truth, simulate.poisson_rois(rng, psf, truth, box)
+
+
+# (bias tolerance, |1 - std/CRLB| tolerance), test/validation_utils_roibatch.jl:74-75, 161-165;
+# the x, y bias always passes there (it depends on the corners)
+ASTIG_TOL = {"x": (None, 0.25), "y": (None, 0.25), "z": (0.03, 0.25),
+             "photons": (100.0, 0.25), "bg": (2.0, 0.25)}
+
+
+def check_astig_validation(fit, n: int = 1000, box: int = 15) -> dict:
+    """Bias and std/CRLB of the astigmatic fit, the reference's
+    validate_roibatch_fitting (test/validation_utils_roibatch.jl:63-171) with
+    its default fitter constraints (z in [-1, 1] um, step 0.1)."""
+    psf, truth, data = astig_validation_data(n, box)
+    cons = default_constraints(psf, 11)
+    ones = np.ones(n, np.int32)
+    params, crlb = fit(3, box, 0, psf, data, ones, ones, None, cons)
+    out = {}
+    for k, name in enumerate(psf.param_names):
+        err = params[:, k].astype(np.float64) - truth[:, k]
+        bias = float(err.mean())
+        c = crlb[:, k][np.isfinite(crlb[:, k])]
+        ratio = float(err.std(ddof=1) / c.mean())
+        btol, stol = ASTIG_TOL[name]
+        out[name] = {"bias": bias, "std_ratio": ratio,
+                     "pass": (btol is None or abs(bias) < btol) and abs(1 - ratio) < stol}
     return out
 
 

@@ -123,8 +123,8 @@ def test_corners_outside_the_map_are_rejected(ctx):
 def test_unsupported_shapes_and_models(ctx):
     w = make_case("xynb-11-poisson", 0, 11, 0, 4)
     desc = make_desc(w.psf, 11, 20, w.constraints, 0)
-    desc.box = 8
-    st, _ = host_fit(ctx, desc, np.zeros((8, 8, 4), np.float32))
+    desc.box = 65  # boxes 3..64 are fitted
+    st, _ = host_fit(ctx, desc, np.zeros((65, 65, 4), np.float32))
     assert st == 3  # GMLE_UNSUPPORTED_BOX
     desc.box, desc.model = 11, 9
     st, _ = host_fit(ctx, desc, w.data)

@@ -40,7 +40,10 @@ def test_erf_exp_rcp_accuracy(ctx):
     print(f"\nerf: fit max |err| {e_fast.max():.3e}, erff max |err| {e_lib.max():.3e}")
     assert e_fast.max() <= 5e-7
     assert np.abs(o[0] - o[1]).max() <= 6e-7
-    assert np.all(np.sign(o[0]) == np.sign(x)) or np.all(np.abs(o[0][np.sign(o[0]) != np.sign(x)]) == 0)
+    # the sign is right except within the error bound of 0 (erf(x) ~ 1.13 x
+    # for |x| < 1e-7, where 1 - e t P(t) rounds to +-6e-8)
+    wrong = np.sign(o[0]) != np.sign(x)
+    assert np.all(np.abs(o[0][wrong]) <= 1.2e-7) and np.all(np.abs(x[wrong]) <= 1e-6)
     g = np.exp(-0.5 * x.astype(np.float64) ** 2)
     big = g > 1e-30
     rel = np.abs(o[2][big] - g[big]) / g[big]

@@ -54,6 +54,12 @@ def test_model_validation_protocol(model):
     assert all(v["pass"] for v in res.values()), res
 
 
+def test_astigmatic_validation_protocol():
+    """test/model_validation_tests.jl:97-135 on the FP32 oracle."""
+    res = SC.check_astig_validation(oracle_fit)
+    assert all(v["pass"] for v in res.values()), res
+
+
 def test_scmos_photometry_protocol():
     res = SC.check_scmos_photometry(oracle_fit)
     assert res["pass"], res
