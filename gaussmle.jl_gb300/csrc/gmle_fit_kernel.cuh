@@ -1772,8 +1772,8 @@ __global__ void __launch_bounds__(128) fit_kernel_r1(const KernelArgs a, const T
 // ---- kernel 2: several threads per ROI ------------------------------------------
 //
 // For batches too small to fill the GPU with one thread per ROI.  TPR lanes
-// (2, 4 or 8) of one warp share a ROI as a grid of NCX column blocks by NRY
-// row blocks (2 x 1, 2 x 2, 4 x 2): lane (rx, ry) owns columns
+// (4 or 8) of one warp share a ROI as a grid of NCX column blocks by NRY row
+// blocks (4 x 1, 4 x 2): lane (rx, ry) owns columns
 // [rx BOX / NCX, (rx + 1) BOX / NCX) and rows [ry BOX / NRY, (ry + 1) BOX / NRY)
 // of the ROI, evaluates the edge tables of its own columns and rows only, and
 // sums its own pixels.  The column and row terms of the gradient and Hessian
@@ -1783,10 +1783,13 @@ __global__ void __launch_bounds__(128) fit_kernel_r1(const KernelArgs a, const T
 // Fisher matrix and the log-likelihood) are combined across the lanes, by
 // warp shuffles.  Every lane then takes the same Newton step, so theta stays
 // identical in all of them.  The initial estimate is computed by every lane
-// from the staged ROI, in the reference's order.
+// from the staged ROI, in the reference's order.  As in the one-thread
+// kernel, the next column's table entry is evaluated ahead of the current
+// column's pixels, and whole columns of rows are independent work: a lane
+// alone on its scheduler is bound by these chains' latency, not by issue.
 template <int TPR> struct LaneGrid {
-    static_assert(TPR == 2 || TPR == 4 || TPR == 8, "2, 4 or 8 lanes per ROI");
-    static constexpr int NCX = TPR == 2 ? 2 : TPR == 4 ? 2 : 4;
+    static_assert(TPR == 4 || TPR == 8, "4 or 8 lanes per ROI");
+    static constexpr int NCX = 4;
     static constexpr int NRY = TPR / NCX;
 };
 
@@ -1864,6 +1867,8 @@ __device__ __forceinline__ void fit_rois_tpr(const KernelArgs &a, int64_t roi0, 
             }
         }
         EdgeWalk wx = walk_start(c0 + 1, ax);
+        float xp, xd1, xd2, xs1 = 0.f, xs2 = 0.f;  // the lane's current column
+        walk_entry<SIG, true>(c0 + 1, ax, wx, xp, xd1, xd2, xs1, xs2);
 
         if (!final_pass) {
             float py2[RMAX], aG[CROSS ? RMAX : 1], C[RMAX], D[RMAX];
@@ -1880,8 +1885,9 @@ __device__ __forceinline__ void fit_rois_tpr(const KernelArgs &a, int64_t roi0, 
             auto columns = [&](auto uncapped_tag) {
                 constexpr bool UNCAPPED = decltype(uncapped_tag)::value;
                 for (int j = c0 + 1; j <= c1; j++) {
-                    float xp, xd1, xd2, xs1 = 0.f, xs2 = 0.f;
-                    walk_entry<SIG, true>(j, ax, wx, xp, xd1, xd2, xs1, xs2);
+                    // next column's entry: independent of this column's pixels
+                    float nxp, nxd1, nxd2, nxs1 = 0.f, nxs2 = 0.f;
+                    walk_entry<SIG, true>(j + 1, ax, wx, nxp, nxd1, nxd2, nxs1, nxs2);
                     const float npx = N * xp, xp2 = xp * xp;
                     const float *col = pix + ((j - 1) * BOX + r0) * PS;
                     float A[2] = {0.f, 0.f}, B[2] = {0.f, 0.f}, E[2] = {0.f, 0.f},
@@ -1912,6 +1918,7 @@ __device__ __forceinline__ void fit_rois_tpr(const KernelArgs &a, int64_t roi0, 
                     col_terms<MODEL, P>(gs, hs, xp, xd1, xd2, xs1, xs2, A[0] + A[1],
                                         B[0] + B[1], E[0] + E[1], F[0] + F[1], Gc[0] + Gc[1],
                                         ax, aw);
+                    xp = nxp; xd1 = nxd1; xd2 = nxd2; xs1 = nxs1; xs2 = nxs2;
                 }
             };
             if constexpr (!SCMOS) {
@@ -1942,8 +1949,8 @@ __device__ __forceinline__ void fit_rois_tpr(const KernelArgs &a, int64_t roi0, 
 #pragma unroll
                 for (int l = 0; l < P; l++) { Fh[k][l] = 0.f; Fl[k][l] = 0.f; }
             for (int j = c0 + 1; j <= c1; j++) {
-                float xp, xd1, xd2, xs1 = 0.f, xs2 = 0.f;
-                walk_entry<SIG, false>(j, ax, wx, xp, xd1, xd2, xs1, xs2);
+                float nxp, nxd1, nxd2, nxs1 = 0.f, nxs2 = 0.f;
+                walk_entry<SIG, false>(j + 1, ax, wx, nxp, nxd1, nxd2, nxs1, nxs2);
                 const float npx = N * xp;
                 const float *col = pix + ((j - 1) * BOX + r0) * PS;
                 float Q[NB][NB];
@@ -1966,6 +1973,7 @@ __device__ __forceinline__ void fit_rois_tpr(const KernelArgs &a, int64_t roi0, 
                                                 llr, Q);
                 }
                 fisher_column<MODEL, P, NB>(Fh, Fl, Q, xp, xd1, xs1, aw);
+                xp = nxp; xd1 = nxd1; xs1 = nxs1;
             }
             llr = group_sum(llr, TPR);
             double Fm[P][P];

@@ -74,6 +74,10 @@ struct Request {
     // copy issued), joined a step (its copy had landed), step launched
     Clock::time_point t_admit, t_join, t_launch;
     int64_t step_id = -1;
+    // GPU times (timed events, trace only): input copy start and end, and
+    // the end of the request's step, in ms after the server's base event
+    cudaEvent_t ev_in0 = nullptr;
+    float g_copy0 = -1.f, g_copy1 = -1.f, g_step = -1.f;
     ReqState state = PENDING;
     gmle_status status = GMLE_OK;
 };
@@ -168,9 +172,12 @@ struct Server {
         int64_t n, step;
         int kind;
         double submit, admit, join, launch, done;  // ms since the server started
+        float copy0, copy1, gstep;                 // GPU ms after ev_base
     };
     std::vector<TraceRow> trace;
     Clock::time_point t_start;
+    cudaEvent_t ev_base = nullptr;  // trace only: recorded on the input stream at start
+    bool tracing() const { return !trace_path.empty(); }
 
     void trace_request(const Request *r)
     {
@@ -178,19 +185,25 @@ struct Server {
         auto ms = [&](Clock::time_point t) {
             return std::chrono::duration<double, std::milli>(t - t_start).count();
         };
+        float c0 = -1.f, c1 = -1.f;
+        if (r->ev_in0 && cudaEventElapsedTime(&c0, ev_base, r->ev_in0) != cudaSuccess) c0 = -1.f;
+        if (cudaEventElapsedTime(&c1, ev_base, r->ev_in) != cudaSuccess) c1 = -1.f;
+        cudaGetLastError();
         trace.push_back({r->ticket, r->host.n, r->step_id, kind_of(r->host.desc), ms(r->t_submit),
-                         ms(r->t_admit), ms(r->t_join), ms(r->t_launch), ms(r->t_done)});
+                         ms(r->t_admit), ms(r->t_join), ms(r->t_launch), ms(r->t_done), c0, c1,
+                         r->g_step});
     }
     void write_trace() const
     {
         if (trace_path.empty()) return;
         FILE *f = std::fopen(trace_path.c_str(), "w");
         if (!f) return;
-        std::fprintf(f, "ticket,n,kind,step,submit_ms,admit_ms,join_ms,launch_ms,done_ms\n");
+        std::fprintf(f, "ticket,n,kind,step,submit_ms,admit_ms,join_ms,launch_ms,done_ms,"
+                        "gpu_copy_start_ms,gpu_copy_end_ms,gpu_step_end_ms\n");
         for (const TraceRow &t : trace)
-            std::fprintf(f, "%llu,%lld,%d,%lld,%.4f,%.4f,%.4f,%.4f,%.4f\n",
+            std::fprintf(f, "%llu,%lld,%d,%lld,%.4f,%.4f,%.4f,%.4f,%.4f,%.4f,%.4f,%.4f\n",
                          (unsigned long long)t.ticket, (long long)t.n, t.kind, (long long)t.step,
-                         t.submit, t.admit, t.join, t.launch, t.done);
+                         t.submit, t.admit, t.join, t.launch, t.done, t.copy0, t.copy1, t.gstep);
         std::fclose(f);
     }
 
@@ -202,7 +215,7 @@ struct Server {
             return e;
         }
         cudaEvent_t e = nullptr;
-        cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&e, tracing() ? cudaEventDefault : cudaEventDisableTiming);
         return e;
     }
     void put_event(cudaEvent_t e)
@@ -285,6 +298,7 @@ struct Server {
     cudaError_t issue_in(Request *r)
     {
         const int64_t n = r->host.n, b2 = (int64_t)r->host.desc.box * r->host.desc.box;
+        if (r->ev_in0) cudaEventRecord(r->ev_in0, s_in);  // trace only
         cudaError_t e = cudaMemcpyAsync((void *)r->dev.data, r->host.data, 4 * n * b2,
                                         cudaMemcpyHostToDevice, s_in);
         if (e == cudaSuccess && r->host.desc.camera != GMLE_CAMERA_POISSON && !r->direct_corners) {
@@ -383,7 +397,10 @@ struct Server {
                 ctx->launches++;
             }
             cudaEvent_t &ev = launch_done[slot][L.kind];
-            if (!ev) GMLE_CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
+            if (!ev)
+                GMLE_CK(cudaEventCreateWithFlags(&ev, tracing() ? cudaEventDefault
+                                                                : cudaEventDisableTiming),
+                        "cudaEventCreate");
             GMLE_CK(cudaEventRecord(ev, q), "cudaEventRecord");
             done.push_back(ev);
         }
@@ -476,6 +493,15 @@ struct Server {
                     continue;
                 }
                 std::vector<Request *> reqs = std::move(it->reqs);
+                if (tracing()) {
+                    float gs = -1.f;
+                    for (cudaEvent_t e : it->done) {
+                        float t = -1.f;
+                        if (cudaEventElapsedTime(&t, ev_base, e) == cudaSuccess) gs = std::max(gs, t);
+                    }
+                    cudaGetLastError();
+                    for (Request *r : reqs) r->g_step = gs;
+                }
                 slot_busy[it->slot] = false;
                 it = inflight.erase(it);
                 lk.unlock();
@@ -550,9 +576,11 @@ void server_destroy(gmle_ctx *ctx)
     for (auto &kv : S->table) {
         if (kv.second->ev_in) cudaEventDestroy(kv.second->ev_in);
         if (kv.second->ev_out) cudaEventDestroy(kv.second->ev_out);
+        if (kv.second->ev_in0) cudaEventDestroy(kv.second->ev_in0);
         delete kv.second;
     }
     for (cudaEvent_t e : S->event_pool) cudaEventDestroy(e);
+    if (S->ev_base) cudaEventDestroy(S->ev_base);
     cudaFree(S->arena.base);
     delete S;
     ctx->server = nullptr;
@@ -629,20 +657,23 @@ gmle_status gmle_server_start(gmle_ctx *ctx, const gmle_server_config *config)
         server_destroy(ctx);
         return fail(ctx, GMLE_CUDA_ERROR, "cannot create the serving streams and buffers");
     }
+    // a request timeline for diagnosis, written when the server stops
+    if (const char *tp = std::getenv("GMLE_SERVER_TRACE")) {
+        S->trace_path = tp;
+        S->trace.reserve(1 << 16);
+        if (cudaEventCreate(&S->ev_base) == cudaSuccess) cudaEventRecord(S->ev_base, S->s_in);
+    }
+    S->t_start = Clock::now();
     // what the loop would otherwise grow while it holds its lock: the latency
     // record, the ticket table and the request events
     S->lat_ms.reserve(kLatencyRecord);
     S->table.reserve(1 << 14);
     for (int k = 0; k < 512; k++) {
         cudaEvent_t e = nullptr;
-        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess) S->event_pool.push_back(e);
+        if (cudaEventCreateWithFlags(&e, S->tracing() ? cudaEventDefault : cudaEventDisableTiming) ==
+            cudaSuccess)
+            S->event_pool.push_back(e);
     }
-    // a request timeline for diagnosis, written when the server stops
-    if (const char *tp = std::getenv("GMLE_SERVER_TRACE")) {
-        S->trace_path = tp;
-        S->trace.reserve(1 << 16);
-    }
-    S->t_start = Clock::now();
     S->th = std::thread([S] { S->loop(); });
     return GMLE_OK;
 }
@@ -725,6 +756,7 @@ gmle_status gmle_submit(gmle_ctx *ctx, const gmle_group *request, uint64_t *tick
         }
         r->ev_in = S->get_event();
         r->ev_out = S->get_event();
+        if (S->tracing()) r->ev_in0 = S->get_event();
         r->ticket = S->next_ticket++;
         S->table[r->ticket] = r;
         S->pending.push_back(r);
@@ -745,6 +777,7 @@ static gmle_status finish_locked(Server *S, Request *r)
     S->table.erase(r->ticket);
     S->put_event(r->ev_in);
     S->put_event(r->ev_out);
+    S->put_event(r->ev_in0);
     delete r;
     return st;
 }

@@ -59,7 +59,7 @@ typedef struct {
 
 /* largest ROI edge the oracle takes (the reference accepts any box >= 3,
  * src/interface.jl:22) */
-#define ORACLE_MAX_BOX 32
+#define ORACLE_MAX_BOX 64
 
 static inline int oracle_nparams(int model)
 {
