@@ -1480,6 +1480,52 @@ __device__ __forceinline__ void write_result(const KernelArgs &a, int64_t roi, b
     }
 }
 
+// The results of a warp's 32 consecutive ROIs (one per lane), written as
+// contiguous runs.  Each lane's parameters, then its CRLBs, go through the
+// warp's own stage of 32 P floats in shared memory (the pixel slots of its
+// ROIs, whose fits are done), so that a warp store writes 32 consecutive
+// words instead of 32 words P floats apart.  Outputs in the caller's pinned
+// host memory are written over the host link, where scattered 4-byte writes
+// are separate transactions that slow every transfer sharing the link (the
+// serving loop's input copies among them).  g = this lane's slot, nroi = the
+// block's ROIs from roi0; every lane of the warp calls it.
+template <int P>
+__device__ __forceinline__ void write_results_warp(const KernelArgs &a, int64_t roi0, int g,
+                                                   int nroi, bool valid, const float (&th)[P],
+                                                   double (&Fm)[P][P], float llr, float *stage)
+{
+    const float qnan = __int_as_float(0x7fc00000);
+    float cr[P], tv[P];
+    uint8_t fl = 0;
+    if (valid && g < nroi) {
+        fl = crlb_from_fisher<P>(Fm, cr);
+#pragma unroll
+        for (int k = 0; k < P; k++) tv[k] = th[k];
+    } else {
+        // corner outside the calibration map (or an empty slot): no fit
+#pragma unroll
+        for (int k = 0; k < P; k++) { cr[k] = qnan; tv[k] = qnan; }
+        llr = qnan;
+    }
+    const int lane = threadIdx.x & 31;
+    const int w0 = g - lane;                     // the warp's first slot
+    const int nw = min(max(nroi - w0, 0), 32);   // its ROIs
+    const int64_t base = (roi0 + w0) * P;
+#pragma unroll
+    for (int pass = 0; pass < 2; pass++) {
+        __syncwarp();  // the stage is free (pixels read, or the previous pass written)
+#pragma unroll
+        for (int k = 0; k < P; k++) stage[lane * P + k] = pass ? cr[k] : tv[k];
+        __syncwarp();
+        float *out = pass ? a.crlb : a.params;
+        for (int e = lane; e < nw * P; e += 32) out[base + e] = stage[e];
+    }
+    if (g < nroi) {
+        a.llr[roi0 + g] = llr;
+        if (a.flags) a.flags[roi0 + g] = fl;
+    }
+}
+
 template <int MODEL>
 __device__ __forceinline__ void axis_widths(const float *th, const KernelArgs &a, float &sxw,
                                             float &syw, AstigWidths &aw)
@@ -1512,6 +1558,7 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
     constexpr int NB = SIG ? 4 : 3;
     constexpr int LW = TmemVar<BOX>::LW;
     using S = Slots<MODEL>;
+    static_assert(B2 >= P, "a warp's pixel slots stage its results");
 
     const int R = blockDim.x;
     float *spix = smem;
@@ -1722,7 +1769,9 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
                     Fm[k][l] = dd_to_double(Fh[k][l], Fl[k][l]);
                     Fm[l][k] = Fm[k][l];
                 }
-            if (g < nroi) write_result<P>(a, roi0 + g, valid, th, Fm, llr);
+            // the warp's pixel slots (32 box^2 >= 32 P floats) stage its results
+            write_results_warp<P>(a, roi0, g, nroi, valid, th, Fm, llr,
+                                  spix + (size_t)(threadIdx.x & ~31) * B2);
         }
     }
 }
