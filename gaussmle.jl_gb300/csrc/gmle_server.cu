@@ -3,11 +3,12 @@
 //
 // One scheduler thread per context:
 //   submit  -> pending (FIFO)          gmle_submit, any thread
-//   admit   -> arena allocation (device memory budget), ROIs (and corners
-//              not in pinned memory) copied in on the input stream
-//                                                            (admission by HBM)
-//   step    -> every admitted request whose copy has landed joins the next
-//              step: one table launch per (camera family, model, box)
+//   admit   -> arena allocation (device memory budget); ROIs and corners
+//              not in pinned memory copied in on the input stream; those in
+//              pinned memory are read in place by the kernels, so such a
+//              request is ready at once                      (admission by HBM)
+//   step    -> every admitted request that is ready (read in place, or its
+//              copy has landed) joins the next step: one table launch per (camera family, model, box)
 //              present; up to max_inflight_steps steps run concurrently,
 //              their launches spread over a few run streams: one block per
 //              tile, or a replay of a CUDA graph of a persistent launch
@@ -67,6 +68,11 @@ struct Request {
     // (sCMOS requests whose both corner arrays are pinned)
     bool direct_corners = false;
     const int32_t *corner_dev[2] = {};
+    // pixels read in place: the device address of the caller's pinned ROI
+    // data (no input copy; the request is ready when admitted)
+    bool direct_in = false;
+    const float *data_dev = nullptr;
+    bool landed = false;  // nothing to copy in: ready when admitted
     int64_t off = -1, bytes = 0;
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
     Clock::time_point t_submit, t_done;
@@ -186,8 +192,10 @@ struct Server {
             return std::chrono::duration<double, std::milli>(t - t_start).count();
         };
         float c0 = -1.f, c1 = -1.f;
-        if (r->ev_in0 && cudaEventElapsedTime(&c0, ev_base, r->ev_in0) != cudaSuccess) c0 = -1.f;
-        if (cudaEventElapsedTime(&c1, ev_base, r->ev_in) != cudaSuccess) c1 = -1.f;
+        if (!r->landed) {  // a request read in place made no copy
+            if (r->ev_in0 && cudaEventElapsedTime(&c0, ev_base, r->ev_in0) != cudaSuccess) c0 = -1.f;
+            if (cudaEventElapsedTime(&c1, ev_base, r->ev_in) != cudaSuccess) c1 = -1.f;
+        }
         cudaGetLastError();
         trace.push_back({r->ticket, r->host.n, r->step_id, kind_of(r->host.desc), ms(r->t_submit),
                          ms(r->t_admit), ms(r->t_join), ms(r->t_launch), ms(r->t_done), c0, c1,
@@ -223,11 +231,12 @@ struct Server {
         if (e) event_pool.push_back(e);
     }
 
-    static int64_t footprint(const gmle_group &g, bool direct_out, bool direct_corners)
+    static int64_t footprint(const gmle_group &g, bool direct_in, bool direct_out,
+                             bool direct_corners)
     {
         const int64_t n = g.n, b2 = (int64_t)g.desc.box * g.desc.box;
         const int P = nparams(g.desc.model);
-        int64_t b = align256(4 * n * b2);
+        int64_t b = direct_in ? 0 : align256(4 * n * b2);
         if (!direct_out) b += 2 * align256(4 * n * P) + align256(4 * n) + align256(n);
         if (g.desc.camera != GMLE_CAMERA_POISSON && !direct_corners) b += 2 * align256(4 * n);
         return b;
@@ -239,8 +248,12 @@ struct Server {
         const int64_t n = r->host.n, b2 = (int64_t)r->host.desc.box * r->host.desc.box;
         const int P = nparams(r->host.desc.model);
         r->dev = r->host;
-        r->dev.data = reinterpret_cast<float *>(p);
-        p += align256(4 * n * b2);
+        if (r->direct_in) {
+            r->dev.data = r->data_dev;
+        } else {
+            r->dev.data = reinterpret_cast<float *>(p);
+            p += align256(4 * n * b2);
+        }
         if (r->direct_out) {
             r->dev.params = static_cast<float *>(r->out_dev[0]);
             r->dev.crlb = static_cast<float *>(r->out_dev[1]);
@@ -294,13 +307,22 @@ struct Server {
         cv_done.notify_all();
     }
 
-    // Copy a request's inputs in (scheduler thread, lock not held).
+    // Copy a request's inputs in (scheduler thread, lock not held).  A
+    // request whose pixels and corners are all read in place has nothing to
+    // copy and is ready at once.
     cudaError_t issue_in(Request *r)
     {
         const int64_t n = r->host.n, b2 = (int64_t)r->host.desc.box * r->host.desc.box;
+        const bool copy_corners = r->host.desc.camera != GMLE_CAMERA_POISSON && !r->direct_corners;
+        if (r->direct_in && !copy_corners) {
+            r->landed = true;
+            return cudaSuccess;
+        }
         if (r->ev_in0) cudaEventRecord(r->ev_in0, s_in);  // trace only
-        cudaError_t e = cudaMemcpyAsync((void *)r->dev.data, r->host.data, 4 * n * b2,
-                                        cudaMemcpyHostToDevice, s_in);
+        cudaError_t e = cudaSuccess;
+        if (!r->direct_in)
+            e = cudaMemcpyAsync((void *)r->dev.data, r->host.data, 4 * n * b2,
+                                cudaMemcpyHostToDevice, s_in);
         if (e == cudaSuccess && r->host.desc.camera != GMLE_CAMERA_POISSON && !r->direct_corners) {
             e = cudaMemcpyAsync((void *)r->dev.x_corners, r->host.x_corners, 4 * n,
                                 cudaMemcpyHostToDevice, s_in);
@@ -443,13 +465,24 @@ struct Server {
                 std::vector<Request *> step;
                 int64_t rois = 0;
                 int ngroups = 0;
-                // the input copies run in order on one stream: the first one
-                // still in flight ends the search
-                size_t taken = 0;
-                for (; taken < staged.size(); taken++) {
-                    Request *r = staged[taken];
-                    if (rois >= cfg.max_step_rois || ngroups >= kServerTableCap) break;
-                    if (cudaEventQuery(r->ev_in) != cudaSuccess) break;
+                // every admitted request that is ready joins, in FIFO order:
+                // those read in place at once, the others when their input
+                // copy has landed.  The copies run in order on one stream, so
+                // after the first one still in flight only in-place requests
+                // can be ready; they do not wait behind it.
+                bool copies_pending = false;
+                size_t keep = 0;
+                for (size_t q = 0; q < staged.size(); q++) {
+                    Request *r = staged[q];
+                    bool ready = false;
+                    if (rois < cfg.max_step_rois && ngroups < kServerTableCap)
+                        ready = r->landed ||
+                                (!copies_pending && cudaEventQuery(r->ev_in) == cudaSuccess);
+                    if (!ready) {
+                        if (!r->landed) copies_pending = true;
+                        staged[keep++] = r;
+                        continue;
+                    }
                     rois += r->host.n;
                     ngroups++;
                     r->state = RUNNING;
@@ -457,7 +490,7 @@ struct Server {
                     r->step_id = steps;
                     step.push_back(r);
                 }
-                staged.erase(staged.begin(), staged.begin() + taken);
+                staged.resize(keep);
                 if (!step.empty()) {
                     slot_busy[slot] = true;
                     std::vector<cudaEvent_t> done;
@@ -741,7 +774,21 @@ gmle_status gmle_submit(gmle_ctx *ctx, const gmle_group *request, uint64_t *tick
             }
         }
     }
-    r->bytes = Server::footprint(*request, r->direct_out, r->direct_corners);
+    // pixels in pinned memory are read in place by the kernels' staging, so
+    // that the request needs no input copy: the copy engine's queue (one
+    // stream, in order) would otherwise make every later request wait behind
+    // a large or slow copy
+    {
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, request->data) != cudaSuccess) {
+            cudaGetLastError();
+        } else if (at.type == cudaMemoryTypeHost && at.devicePointer != nullptr &&
+                   (reinterpret_cast<uintptr_t>(request->data) & 3) == 0) {
+            r->direct_in = true;
+            r->data_dev = static_cast<const float *>(at.devicePointer);
+        }
+    }
+    r->bytes = Server::footprint(*request, r->direct_in, r->direct_out, r->direct_corners);
     r->t_submit = Clock::now();
     {
         std::lock_guard<std::mutex> lk(S->mu);

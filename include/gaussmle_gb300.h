@@ -352,8 +352,10 @@ gmle_status gmle_fit_mixed_device_noalloc(const gmle_group *groups, int32_t ngro
  * soon as SMs and memory free up.  Results land in the caller's host
  * buffers, which must stay valid until the request completes: outputs in
  * pinned (page-locked) memory are written there by the kernels, others are
- * copied back after the step.  Corner arrays in pinned memory are read in
- * place by the kernels; others are copied in with the pixels.
+ * copied back after the step.  ROI data and corner arrays in pinned memory
+ * are read in place by the kernels (such a request needs no input copy and
+ * can join the next step at once); others are copied in on one input stream,
+ * in order.
  */
 typedef struct {
     int64_t hbm_budget_bytes;   /* device arena; 0 = half of the free HBM at start */
