@@ -53,14 +53,12 @@ WORKLOAD = ("mixed-batch: 40% XYNB 11x11, 25% XYNBS 9x9, 15% XYNBSXSY 13x13, "
 # kernel (dram__bytes_read.sum + dram__bytes_write.sum over the ROIs of the
 # captured launch); the roofline's traffic scales it to the timed launch.
 TRAFFIC_BYTES_PER_ROI: dict[str, float] = {
-    # 90 000 ROIs, 4 threads per ROI, 32 ROIs/block: 150.3 MB read + 5.8 MB written
-    "fit_kernel<3, 15, true, false>": 1734.7,
     # 90 000 ROIs, one thread per ROI, 128 ROIs/block (variances in tensor
-    # memory, per-warp staging): 165.0 MB read + 5.4 MB written
-    "fit_kernel_r1<3, 15, true, false>": 1894.0,
+    # memory, per-warp staging): 166.3 MB read + 5.3 MB written
+    "fit_kernel_r1<3, 15, true, false>": 1907.4,
     # 240 000 ROIs, one thread per ROI, 128 ROIs/block (variances in tensor
-    # memory): 194.9 MB read + 8.9 MB written
-    "fit_kernel_r1<0, 11, true, false>": 849.0,
+    # memory): 199.4 MB read + 8.9 MB written
+    "fit_kernel_r1<0, 11, true, false>": 867.9,
 }
 
 

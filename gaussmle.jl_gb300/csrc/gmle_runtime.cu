@@ -593,20 +593,26 @@ gmle_status gmle_autotune(gmle_ctx *ctx, const gmle_fit_desc *desc, const float 
                 continue;
             KernelArgs a = make_args(ctx, desc, d_data, d_x_corners, d_y_corners, n, d_params,
                                      d_crlb, d_llr, d_flags, tpr);
-            cudaError_t e = launch(ctx, desc, a, rpb, ctx->s_fit);  // warm-up
-            if (e == cudaSuccess) e = cudaEventRecord(e0, ctx->s_fit);
-            for (int rep = 0; rep < 2 && e == cudaSuccess; rep++)
-                e = launch(ctx, desc, a, rpb, ctx->s_fit);
-            if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->s_fit);
-            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-            float ms = 0.f;
-            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            // two warm-up launches, then the fastest of four timed one by one:
+            // a single average was swayed by clock ramps and by other work on
+            // the GPU, and picked slower shapes
+            cudaError_t e = launch(ctx, desc, a, rpb, ctx->s_fit);
+            if (e == cudaSuccess) e = launch(ctx, desc, a, rpb, ctx->s_fit);
+            float ms = 1e30f;
+            for (int rep = 0; rep < 4 && e == cudaSuccess; rep++) {
+                e = cudaEventRecord(e0, ctx->s_fit);
+                if (e == cudaSuccess) e = launch(ctx, desc, a, rpb, ctx->s_fit);
+                if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->s_fit);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                float t = 0.f;
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+                if (e == cudaSuccess) ms = std::min(ms, t);
+            }
             if (e != cudaSuccess) {
                 cudaEventDestroy(e0);
                 cudaEventDestroy(e1);
                 return cuda_fail(ctx, e, "autotune launch");
             }
-            ms *= 0.5f;
             if (ms < best_ms) {
                 best_ms = ms;
                 best = {tpr, rpb};
