@@ -94,6 +94,8 @@ def parse():
     p.add_argument("--tpr", type=int, default=0,
                    help="with --plain: threads per ROI (0: the autotuner's choice)")
     p.add_argument("--rpb", type=int, default=0, help="with --plain: ROIs per block")
+    p.add_argument("--method", default="newton", choices=["newton", "lm"],
+                   help="with --plain: the reference's Newton step, or the full-Hessian option")
     return p.parse_args()
 
 
@@ -375,50 +377,41 @@ def time_steps(torch, stream, fn, steps, warmup):
     return e0.elapsed_time(e1) / 1e3
 
 
+def plain_in_fresh_process(model, box, camera, n, steps, method="newton") -> dict:
+    """One `--plain` measurement in a process of its own: the launch's time
+    does not depend on the workloads this process ran before (in-process, after
+    other workloads, the same compute-bound launch was measured up to 9 %
+    slower, the full-Hessian one up to 1.8x, with the GPU at full clock)."""
+    cmd = [sys.executable, str(ROOT / "bench.py"), "--plain", f"{model},{box},{camera},{n}",
+           "--steps", str(steps), "--warmup", "3", "--method", method]
+    res = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+    if res.returncode != 0:
+        raise RuntimeError(f"plain run {cmd[3:]} failed:\n{res.stderr[-2000:]}")
+    return json.loads(res.stdout.strip().splitlines()[-1])
+
+
 def extras(torch, ctx, dev, steps, peak_inst):
-    """Plain-kernel throughput of the other workloads (device-resident)."""
-    import gaussmle_gb300 as G
-    from gaussmle_gb300 import simulate, roofline
-    from gaussmle_gb300.fitter import make_desc
+    """Plain-kernel throughput of the other workloads (device-resident); the
+    fit workloads each in a fresh process (plain_in_fresh_process)."""
     out = {}
-    stream = torch.cuda.Stream(dev)
     for name, model, box, cam, n in [("xynb-11x11-poisson-10k (reference CPU case)", 0, 11, 0, 10_000),
                                      ("xynb-11x11-poisson-1e6", 0, 11, 0, 1_000_000),
                                      ("xynbs-13x13-scmos-1e6", 1, 13, 2, 1_000_000),
                                      ("astig-15x15-poisson-1e6", 3, 15, 0, 1_000_000)]:
-        wl = simulate.device_workload(model, box, cam, n, device=dev)
-        if cam:
-            set_maps(ctx, wl)
-        psf, P = wl["psf"], wl["psf"].nparams
-        cons = simulate.ASTIG_WIDE if model == 3 else G.default_constraints(psf, 11)
-        desc = make_desc(psf, box, 20, cons, cam)
-        prm = torch.empty((n, P), device=dev)
-        crl = torch.empty((n, P), device=dev)
-        llr = torch.empty(n, device=dev)
-        flg = torch.empty(n, dtype=torch.uint8, device=dev)
-        from gaussmle_gb300 import tuning
-        tpr, rpb, _ = tuning.autotune(ctx, desc, wl["data"], wl["xc"], wl["yc"], prm, crl, llr,
-                                      flg, save=False)
-        dt = time_steps(torch, stream, lambda: G.fit_device(ctx, desc, wl["data"], wl["xc"],
-                                                             wl["yc"], prm, crl, llr, flg,
-                                                             stream=stream), steps, 3)
-        per = dt / steps
-        rl = kernel_roofline(torch, dev, model, box, cam, n, per)
-        out[name] = {"fits_per_s": n / per, "ms_per_launch": per * 1e3,
-                     "shape": [tpr, rpb], "work_slots_per_roi": rl["work_per_roi"]["slots"],
+        r = plain_in_fresh_process(model, box, cam, n, steps)
+        rl = r["roofline"]
+        out[name] = {"fits_per_s": r["fits_per_s"], "ms_per_launch": r["ms_per_launch"],
+                     "shape": r["shape"], "work_slots_per_roi": rl["work_per_roi"]["slots"],
                      "roofline_frac": rl["frac"], "bound": rl["bound"]}
         if name == "xynb-11x11-poisson-1e6":
             # the full-Hessian option (Fisher scoring with LM damping) on the
             # same ROIs, 20 iterations
-            dlm = make_desc(psf, box, 20, cons, cam, 1)
-            dt = time_steps(torch, stream, lambda: G.fit_device(ctx, dlm, wl["data"], wl["xc"],
-                                                                 wl["yc"], prm, crl, llr, flg,
-                                                                 stream=stream), steps, 3)
+            lm = plain_in_fresh_process(model, box, cam, n, steps, "lm")
             out["xynb-11x11-poisson-1e6-fisher-lm"] = {
-                "fits_per_s": n * steps / dt, "ms_per_launch": dt / steps * 1e3,
-                "vs_newton": per / (dt / steps)}
-        del wl, prm, crl, llr, flg
-        torch.cuda.empty_cache()
+                "fits_per_s": lm["fits_per_s"], "ms_per_launch": lm["ms_per_launch"],
+                "vs_newton": r["ms_per_launch"] / lm["ms_per_launch"]}
+    import gaussmle_gb300 as G
+    stream = torch.cuda.Stream(dev)
     # ROI extraction from device-resident frames (gmle_cut_rois_device): an
     # HBM-bound copy; 100 frames of 2048 x 2048 (1.7 GB) and 2e6 11x11 ROIs
     # (0.97 GB out), both larger than L2
@@ -696,7 +689,9 @@ def run_plain(args):
         set_maps(ctx, wl)
     psf, P = wl["psf"], wl["psf"].nparams
     cons = simulate.ASTIG_WIDE if model == 3 else G.default_constraints(psf, 11)
-    desc = make_desc(psf, box, 20, cons, cam)
+    from gaussmle_gb300 import _lib
+    method = _lib.METHOD_FISHER_LM if args.method == "lm" else _lib.METHOD_NEWTON
+    desc = make_desc(psf, box, 20, cons, cam, method)
     prm = torch.empty((n, P), device=dev)
     crl = torch.empty((n, P), device=dev)
     llr = torch.empty(n, device=dev)
@@ -715,7 +710,8 @@ def run_plain(args):
                     args.warmup)
     per = dt / args.steps
     rl = kernel_roofline(torch, dev, model, box, cam, n, per)
-    print(json.dumps({"workload": f"plain model {model} box {box} camera {cam} n {n}",
+    print(json.dumps({"workload": f"plain model {model} box {box} camera {cam} n {n}"
+                                  f" method {args.method}",
                       "fits_per_s": n / per, "ms_per_launch": per * 1e3, "shape": [tpr, rpb],
                       "launches": ctx.launches() - l0, "roofline": rl}))
 

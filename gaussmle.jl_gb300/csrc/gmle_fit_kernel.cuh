@@ -233,7 +233,15 @@ __device__ __forceinline__ EdgeWalk walk_start(int t0, const Axis &a)
 // the factor PSF of the other axis.  The expressions keep the reference's
 // association: (t - c) + 1/2 inside erf and the sigma products, (t + 1/2) - c
 // inside exp.
-template <bool SIG, bool SECOND>
+//
+// VOTE (one-thread-per-ROI kernel only, where a warp's 32 lanes walk in step):
+// the rare re-evaluation of the lower edge's erf sits behind a warp vote, so
+// that it costs issue slots only in the warps that need it.  Measured per
+// kernel (plain launches, sCMOS ADU): astigmatic 15x15 1.874 -> 1.815 ms for
+// 300 000 ROIs, XYNB 7x7 0.153 -> 0.151 ms for 100 000; slower for
+// XYNBSXSY 13x13 (1.331 -> 1.382 ms), XYNB 11x11 (1.791 -> 1.804 ms) and the
+// astigmatic 15x15 Poisson kernel.
+template <bool SIG, bool SECOND, bool VOTE = false>
 __device__ __forceinline__ void walk_entry(int t, const Axis &a, EdgeWalk &w, float &psf,
                                            float &d1, float &d2, float &s1, float &s2)
 {
@@ -246,7 +254,14 @@ __device__ __forceinline__ void walk_entry(int t, const Axis &a, EdgeWalk &w, fl
     const float fb = w.fa;
     const float fa = gauss_edge(ea * a.inv_s);
     float erfb = w.erfa;
-    if (ub != w.ua) erfb = erf_from_gauss(__fmul_rn(ub, a.sq), fb);
+    if (VOTE) {
+        if (__any_sync(0xffffffffu, ub != w.ua)) {
+            const float r = erf_from_gauss(__fmul_rn(ub, a.sq), fb);
+            erfb = ub != w.ua ? r : erfb;
+        }
+    } else if (ub != w.ua) {
+        erfb = erf_from_gauss(__fmul_rn(ub, a.sq), fb);
+    }
     const float erfa = erf_from_gauss(__fmul_rn(ua, a.sq), fa);
     // the true value is >= 0 (erf is increasing and ua > ub), so is the
     // reference's; a negative rounding residue of the tails is cut to 0
@@ -1557,6 +1572,8 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
     constexpr int PS = 1;  // data plane; sCMOS variance tiles are in tensor memory
     constexpr int NB = SIG ? 4 : 3;
     constexpr int LW = TmemVar<BOX>::LW;
+    // edge walks with the warp-voted erf re-evaluation (walk_entry)
+    constexpr bool VOTE = SCMOS && ((MODEL == 3 && BOX >= 15) || BOX <= 7);
     using S = Slots<MODEL>;
     static_assert(B2 >= P, "a warp's pixel slots stage its results");
 
@@ -1609,13 +1626,13 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
 #pragma unroll
             for (int t = 0; t < BOX; t++) {
                 float s1 = 0.f, s2 = 0.f;
-                walk_entry<SIG, true>(t + 1, ay, wy, py[t], yd1[t], yd2[t], s1, s2);
+                walk_entry<SIG, true, VOTE>(t + 1, ay, wy, py[t], yd1[t], yd2[t], s1, s2);
                 if (SIG) { ys1[t] = s1; ys2[t] = s2; }
             }
         }
         EdgeWalk wx = walk_start(1, ax);
         float xp, xd1, xd2, xs1 = 0.f, xs2 = 0.f;
-        walk_entry<SIG, true>(1, ax, wx, xp, xd1, xd2, xs1, xs2);
+        walk_entry<SIG, true, VOTE>(1, ax, wx, xp, xd1, xd2, xs1, xs2);
 
         if (LM && !final_pass) {
             float llr = 0.f;
@@ -1628,7 +1645,7 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
             }
             for (int j = 1; j <= BOX; j++) {
                 float nxp, nxd1, nxd2, nxs1 = 0.f, nxs2 = 0.f;
-                walk_entry<SIG, false>(j + 1, ax, wx, nxp, nxd1, nxd2, nxs1, nxs2);
+                walk_entry<SIG, false, VOTE>(j + 1, ax, wx, nxp, nxd1, nxd2, nxs1, nxs2);
                 const float npx = N * xp;
                 const float *col = pix + (j - 1) * BOX * PS;
                 float vv[LW];  // this column's variances, from tensor memory
@@ -1681,7 +1698,7 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
                 for (int j = 1; j <= BOX; j++) {
                     // next column's table entry: independent of this column's pixels
                     float nxp, nxd1, nxd2, nxs1 = 0.f, nxs2 = 0.f;
-                    walk_entry<SIG, true>(j + 1, ax, wx, nxp, nxd1, nxd2, nxs1, nxs2);
+                    walk_entry<SIG, true, VOTE>(j + 1, ax, wx, nxp, nxd1, nxd2, nxs1, nxs2);
                     const float npx = N * xp, xp2 = xp * xp;
                     const float *col = pix + (j - 1) * BOX * PS;
                     float nv[LW];
@@ -1741,7 +1758,7 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
                 for (int l = 0; l < P; l++) { Fh[k][l] = 0.f; Fl[k][l] = 0.f; }
             for (int j = 1; j <= BOX; j++) {
                 float nxp, nxd1, nxd2, nxs1 = 0.f, nxs2 = 0.f;
-                walk_entry<SIG, false>(j + 1, ax, wx, nxp, nxd1, nxd2, nxs1, nxs2);
+                walk_entry<SIG, false, VOTE>(j + 1, ax, wx, nxp, nxd1, nxd2, nxs1, nxs2);
                 const float npx = N * xp;
                 const float *col = pix + (j - 1) * BOX * PS;
                 float vv[LW];  // this column's variances, from tensor memory
