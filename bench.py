@@ -102,17 +102,68 @@ def parse():
 # ---------------------------------------------------------------------------
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    """SM clock, clock-event (throttle) reasons and power of the GPU, sampled
+    every 5 ms through NVML (read-only queries) in a host thread; begin() and
+    end() mark the timed region, and stop() summarises the samples inside it.
+    Falls back to `nvidia-smi -lms 200` where NVML cannot be loaded."""
+    # nvmlClocksEventReasons bits
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, device_index: int):
+    def __init__(self, device_index: int, pci_bus_id: str | None = None):
         self.idx = device_index
+        self.pci = pci_bus_id
         self.proc = None
         self.path = None
+        self.nvml = None
+        self.samples = []
+        self.t0 = self.t1 = None
+
+    def _open_nvml(self):
+        try:
+            lib = C.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return None
+            h = C.c_void_p()
+            ok = False
+            if self.pci:
+                ok = lib.nvmlDeviceGetHandleByPciBusId_v2(self.pci.encode(), C.byref(h)) == 0
+            if not ok:
+                ok = lib.nvmlDeviceGetHandleByIndex_v2(self.idx, C.byref(h)) == 0
+            if not ok:
+                return None
+            reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                lib.nvmlDeviceGetCurrentClocksThrottleReasons
+            mx = C.c_uint()
+            lib.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx))  # NVML_CLOCK_SM
+            self.max_mhz = float(mx.value)
+            return lib, h, reasons
+        except (OSError, AttributeError):
+            return None
+
+    def _run(self):
+        lib, h, reasons = self.nvml
+        clk, mask, mw = C.c_uint(), C.c_ulonglong(), C.c_uint()
+        while not self._stop.is_set():
+            t = time.perf_counter()
+            if lib.nvmlDeviceGetClockInfo(h, 1, C.byref(clk)) == 0 and \
+                    reasons(h, C.byref(mask)) == 0:
+                p = mw.value / 1e3 if lib.nvmlDeviceGetPowerUsage(h, C.byref(mw)) == 0 else None
+                self.samples.append((t, float(clk.value), int(mask.value), p))
+            self._stop.wait(0.005)
 
     def start(self):
+        import threading
+        self.nvml = self._open_nvml()
+        if self.nvml is not None:
+            self._stop = threading.Event()
+            self._thread = threading.Thread(target=self._run, daemon=True)
+            self._thread.start()
+            time.sleep(0.05)
+            return
         fd, self.path = tempfile.mkstemp(suffix=".csv")
         os.close(fd)
         try:
@@ -123,7 +174,30 @@ class ClockSampler:
         except FileNotFoundError:
             self.proc = None
 
+    def begin(self):
+        self.t0 = time.perf_counter()
+
+    def end(self):
+        self.t1 = time.perf_counter()
+
     def stop(self) -> dict:
+        if self.nvml is not None:
+            self._stop.set()
+            self._thread.join()
+            lo, hi = self.t0 or 0.0, self.t1 or float("inf")
+            inside = [x for x in self.samples if lo <= x[0] <= hi]
+            if not inside:
+                return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": ["no samples"],
+                        "samples": 0, "source": "nvml"}
+            masks = 0
+            for x in inside:
+                masks |= x[2]
+            pw = [x[3] for x in inside if x[3] is not None]
+            return {"sm_mhz": statistics.median(x[1] for x in inside),
+                    "sm_min_mhz": min(x[1] for x in inside), "sm_max_mhz": self.max_mhz,
+                    "reasons": sorted(v for k, v in self.REASONS.items() if masks & k),
+                    "power_w_median": statistics.median(pw) if pw else None,
+                    "samples": len(inside), "source": "nvml, 5 ms, inside the timed region"}
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -143,7 +217,16 @@ class ClockSampler:
                           if r[5 + k].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(rows)}
+                "samples": len(rows), "source": "nvidia-smi, 200 ms"}
+
+
+def pci_bus_id(torch, dev) -> str | None:
+    """The device's PCI address in NVML's form, where torch reports it."""
+    p = torch.cuda.get_device_properties(dev)
+    try:
+        return f"{p.pci_domain_id:08x}:{p.pci_bus_id:02x}:{p.pci_device_id:02x}.0"
+    except AttributeError:
+        return None
 
 
 def fp32_peak_tinst(torch, dev) -> float:
@@ -490,18 +573,20 @@ def run_ours(args):
         step()
     torch.cuda.synchronize()
     launches0 = ctx.launches()
-    sampler = ClockSampler(local)
+    sampler = ClockSampler(local, pci_bus_id(torch, dev))
     sampler.start()
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.nvtx.range_push("value")  # the timed region, for profiler filters
+    sampler.begin()
     e0.record(stream)
     for _ in range(args.steps):
         step()
     e1.record(stream)
     torch.cuda.synchronize()
+    sampler.end()
     torch.cuda.nvtx.range_pop()
     clocks = sampler.stop()
     dt = max_over_ranks(e0.elapsed_time(e1) / 1e3, world, dev)

@@ -239,6 +239,16 @@ def generate_roi_batch(camera, psf_microns: PSFModel, n_rois: int, roi_size: int
 
 # ---- on-device generation (benchmark inputs at 10^6 ROIs) --------------------
 
+def _poisson_t(torch, mu, g):
+    """torch.poisson on the device, after a host-side check that every rate is
+    finite and >= 0: torch's kernel stops the device on an invalid rate (a
+    device-side assert), the check raises an exception instead."""
+    bad = int((~torch.isfinite(mu) | (mu < 0)).sum().item())
+    if bad:
+        raise RuntimeError(f"{bad} of {mu.numel()} Poisson rates are negative or not finite")
+    return torch.poisson(mu, generator=g)
+
+
 def _psf_1d_t(torch, centre, sigma, box):
     t = torch.arange(1, box + 1, dtype=torch.float64, device=centre.device)[None, :]
     c = centre.double()[:, None]
@@ -270,7 +280,7 @@ def xynbs13_scmos_device(n: int = 1_000_000, seed: int = 1001, sensor: int = 204
     px = _psf_1d_t(torch, x, s, box)                      # (n, box) columns j
     py = _psf_1d_t(torch, y, s, box)                      # (n, box) rows i
     mu = bg[:, None, None] + N[:, None, None] * px[:, :, None] * py[:, None, :]  # (n, j, i)
-    e = torch.poisson(mu, generator=g)
+    e = _poisson_t(torch, mu, g)
     jj = torch.arange(box, device=device)[None, :, None]
     ii = torch.arange(box, device=device)[None, None, :]
     cols = (xc.long()[:, None, None] - 1) + jj
@@ -320,7 +330,7 @@ def device_workload(model: int, box: int, camera: int, n: int, seed: int = 2024,
     px = _psf_1d_t(torch, x, sx, box)
     py = _psf_1d_t(torch, y, sy, box)
     mu = bg[:, None, None] + N[:, None, None] * px[:, :, None] * py[:, None, :]
-    e = torch.poisson(mu, generator=g)
+    e = _poisson_t(torch, mu, g)
     out = {"truth": truth.float(), "box": box, "n": n, "psf": psf, "model": model,
            "camera": camera, "ny": 0, "nx": 0, "xc": None, "yc": None}
     if camera:
@@ -389,7 +399,7 @@ def mixed_batch_scmos_device(n: int = 2_000_000, seed: int = 1003, sensor: int =
         px = _psf_1d_t(torch, x, sx, box)
         py = _psf_1d_t(torch, y, sy, box)
         mu = bg[:, None, None] + N[:, None, None] * px[:, :, None] * py[:, None, :]
-        e = torch.poisson(mu, generator=g)
+        e = _poisson_t(torch, mu, g)
         xc = torch.randint(1, sensor - box + 2, (cnt,), generator=g, device=device, dtype=torch.int32)
         yc = torch.randint(1, sensor - box + 2, (cnt,), generator=g, device=device, dtype=torch.int32)
         jj = torch.arange(box, device=device)[None, :, None]
