@@ -1838,8 +1838,8 @@ __global__ void __launch_bounds__(128) fit_kernel_r1(const KernelArgs a, const T
 // ---- kernel 2: several threads per ROI ------------------------------------------
 //
 // For batches too small to fill the GPU with one thread per ROI.  TPR lanes
-// (4 or 8) of one warp share a ROI as a grid of NCX column blocks by NRY row
-// blocks (4 x 1, 4 x 2): lane (rx, ry) owns columns
+// (2, 4 or 8) of one warp share a ROI as a grid of NCX column blocks by NRY row
+// blocks (2 x 1, 4 x 1, 4 x 2): lane (rx, ry) owns columns
 // [rx BOX / NCX, (rx + 1) BOX / NCX) and rows [ry BOX / NRY, (ry + 1) BOX / NRY)
 // of the ROI, evaluates the edge tables of its own columns and rows only, and
 // sums its own pixels.  The column and row terms of the gradient and Hessian
@@ -1853,9 +1853,15 @@ __global__ void __launch_bounds__(128) fit_kernel_r1(const KernelArgs a, const T
 // kernel, the next column's table entry is evaluated ahead of the current
 // column's pixels, and whole columns of rows are independent work: a lane
 // alone on its scheduler is bound by these chains' latency, not by issue.
+//
+// Two lanes (measured at 10 000 XYNB 11x11 ROIs): with about one warp per
+// scheduler, a lane's time is its instruction count over the single-warp
+// issue rate, and two column blocks halve the pixel work while only the y
+// tables are evaluated twice.  Four lanes cut a lane's instructions further
+// but add 79 % to the ROI's total and share each scheduler between two warps.
 template <int TPR> struct LaneGrid {
-    static_assert(TPR == 4 || TPR == 8, "4 or 8 lanes per ROI");
-    static constexpr int NCX = 4;
+    static_assert(TPR == 2 || TPR == 4 || TPR == 8, "2, 4 or 8 lanes per ROI");
+    static constexpr int NCX = TPR == 2 ? 2 : 4;
     static constexpr int NRY = TPR / NCX;
 };
 

@@ -6,8 +6,8 @@
 // parallel):
 //   part 0  one thread per ROI (fit_kernel_r1), odd boxes 5..15;
 //   part 1  one thread per ROI, boxes 3, 4, 6, 8, 10, 12, 14, 16;
-//   part 2  several lanes per ROI (fit_kernel): 4 and 8 lanes for odd boxes
-//           5..15, 4 lanes for the others.
+//   part 2  several lanes per ROI (fit_kernel): 2, 4 and 8 lanes for odd
+//           boxes 5..15, 4 lanes for the others.
 // Other translation units see the parts through extern template declarations.
 #pragma once
 
@@ -51,10 +51,10 @@ struct LaunchShape {
 };
 
 // Lanes per ROI with a compiled kernel: 1 (fit_kernel_r1) for every box; 4
-// (fit_kernel) for every box; 8 for the odd boxes 5..15.
+// (fit_kernel) for every box; 2 and 8 for the odd boxes 5..15.
 inline bool tpr_supported(int tpr, int box)
 {
-    return tpr == 1 || tpr == 4 || (tpr == 8 && main_box(box));
+    return tpr == 1 || tpr == 4 || ((tpr == 2 || tpr == 8) && main_box(box));
 }
 
 // Part holding the kernel of a launch shape (see the top of this file).
@@ -138,21 +138,26 @@ cudaError_t kernel_for(int tpr, bool table, bool lm, FitKernel *kern)
         else *kern = table ? fit_kernel_r1<MODEL, BOX, SCMOS, true> : fit_kernel_r1<MODEL, BOX, SCMOS, false>;
     } else if constexpr (PART == 2) {
         if (r1) return cudaErrorInvalidConfiguration;
-        if (tpr == 4) *kern = table ? fit_kernel<MODEL, BOX, SCMOS, true, 4> : fit_kernel<MODEL, BOX, SCMOS, false, 4>;
-        else if constexpr (main_box(BOX))
-            *kern = table ? fit_kernel<MODEL, BOX, SCMOS, true, 8> : fit_kernel<MODEL, BOX, SCMOS, false, 8>;
+        if (tpr == 4) {
+            *kern = table ? fit_kernel<MODEL, BOX, SCMOS, true, 4> : fit_kernel<MODEL, BOX, SCMOS, false, 4>;
+        } else if constexpr (main_box(BOX)) {
+            if (tpr == 2)
+                *kern = table ? fit_kernel<MODEL, BOX, SCMOS, true, 2> : fit_kernel<MODEL, BOX, SCMOS, false, 2>;
+            else
+                *kern = table ? fit_kernel<MODEL, BOX, SCMOS, true, 8> : fit_kernel<MODEL, BOX, SCMOS, false, 8>;
+        }
     } else {
         return cudaErrorInvalidConfiguration;
     }
     // The largest dynamic shared memory a block may have, once per kernel and
     // device (setting it twice is harmless).
     constexpr int kMaxDevices = 64;
-    static bool done[2][3][2][kMaxDevices] = {};
+    static bool done[2][4][2][kMaxDevices] = {};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     const bool known = dev >= 0 && dev < kMaxDevices;
-    const int ti = tpr == 1 ? 0 : tpr == 4 ? 1 : 2;
+    const int ti = tpr == 1 ? 0 : tpr == 2 ? 1 : tpr == 4 ? 2 : 3;
     if (known && done[lm][ti][table][dev]) return cudaSuccess;
     // the 227 KiB a block may use include the kernel's static shared memory
     cudaFuncAttributes fa;

@@ -517,7 +517,7 @@ gmle_status gmle_set_tuning(gmle_ctx *ctx, int32_t model, int32_t box, int32_t c
         return fail(ctx, GMLE_UNSUPPORTED_BOX, "box %d has no launch-shape choice (3..16)", box);
     if (!gmle::tpr_supported(tpr, box))
         return fail(ctx, GMLE_INVALID_ARG,
-                    "threads_per_roi must be 1, 4, or 8 (8: odd boxes 5..15 only)");
+                    "threads_per_roi must be 1, 2, 4, or 8 (2 and 8: odd boxes 5..15 only)");
     const bool scmos = camera != GMLE_CAMERA_POISSON;
     const int threads = tpr * rois_per_block;
     if (rois_per_block < 1 || threads > (tpr == 1 ? gmle::kMaxThreadsR1 : 256) || threads % 32)
@@ -583,7 +583,7 @@ gmle_status gmle_autotune(gmle_ctx *ctx, const gmle_fit_desc *desc, const float 
     // (three warps: two such blocks of large sCMOS ROIs fit where one of four
     // warps does)
     static const int kThreads[] = {32, 64, 96, 128, 256};
-    for (int tpr : {1, 4, 8}) {
+    for (int tpr : {1, 2, 4, 8}) {
         if (!gmle::tpr_supported(tpr, desc->box)) continue;
         for (int threads : kThreads) {
             if (threads > (tpr == 1 ? gmle::kMaxThreadsR1 : 256)) continue;

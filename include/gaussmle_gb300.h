@@ -167,7 +167,7 @@ gmle_status gmle_fit_device_errors(gmle_ctx *ctx, int64_t *count);
  * Kernel launch shape used for a (model, box, camera): threads per ROI and
  * ROIs per block, as picked by the autotuner (or set by gmle_set_tuning;
  * setting (0, 0) forgets the entry and restores the size-based default).
- * Threads per ROI: 1, 4, or 8 (8 for odd boxes 5..15 only); one thread per
+ * Threads per ROI: 1, 2, 4, or 8 (2 and 8 for odd boxes 5..15 only); one thread per
  * ROI allows at most 128 ROIs per block, several lanes 256 threads per block.
  * Boxes 3..16; larger boxes run in one fixed shape.
  */
@@ -177,7 +177,7 @@ gmle_status gmle_set_tuning(gmle_ctx *ctx, int32_t model, int32_t box, int32_t c
                             int32_t threads_per_roi, int32_t rois_per_block);
 
 /*
- * Autotuner: times every candidate launch shape (threads per ROI 1, 4, 8;
+ * Autotuner: times every candidate launch shape (threads per ROI 1, 2, 4, 8;
  * 32..256 threads per block, within 227 KiB of shared memory) of the fit
  * kernel for `desc` on a device-resident batch, keeps the fastest for
  * (model, box, camera family) in the context and returns it with its time

@@ -65,9 +65,25 @@ def test_new_boxes_every_launch_shape(ctx, model, box, camera, tpr, rpb):
     check(w, params, crlb, flags)
 
 
-def test_eight_lanes_are_for_odd_boxes_only(ctx):
+@pytest.mark.parametrize("rpb", [16, 64, 128])
+@pytest.mark.parametrize("model,box,camera", [(0, 11, 0), (1, 9, 2), (2, 13, 1), (3, 15, 2),
+                                              (0, 5, 0), (0, 7, 2)])
+def test_two_lanes_per_roi(ctx, model, box, camera, rpb):
+    """Two lanes per ROI (two column blocks; the odd boxes 5..15)."""
+    w = make_case(f"m{model}-{box}-{camera}", model, box, camera, 500)
+    ctx.check(ctx.lib.gmle_set_tuning(ctx.handle, model, box, camera, 2, rpb))
+    try:
+        params, crlb, llr, flags = run_gpu(ctx, w)
+    finally:
+        ctx.check(ctx.lib.gmle_set_tuning(ctx.handle, model, box, camera, 0, 0))
+    check(w, params, crlb, flags)
+
+
+def test_two_and_eight_lanes_are_for_odd_boxes_only(ctx):
     assert ctx.lib.gmle_set_tuning(ctx.handle, 0, 8, 0, 8, 16) == 1  # GMLE_INVALID_ARG
+    assert ctx.lib.gmle_set_tuning(ctx.handle, 0, 8, 0, 2, 16) == 1
     assert ctx.lib.gmle_set_tuning(ctx.handle, 0, 9, 0, 8, 16) == 0
+    assert ctx.lib.gmle_set_tuning(ctx.handle, 0, 9, 0, 2, 16) == 0
     ctx.check(ctx.lib.gmle_set_tuning(ctx.handle, 0, 9, 0, 0, 0))
 
 

@@ -182,7 +182,7 @@ def test_autotune_picks_a_valid_shape(ctx):
     desc = make_desc(w.psf, 11, 20, w.constraints, 0)
     try:
         tpr, rpb, ms = tuning.autotune(ctx, desc, data, None, None, *out, save=False)
-        assert tpr in (1, 4, 8) and (tpr * rpb) % 32 == 0 and ms > 0
+        assert tpr in (1, 2, 4, 8) and (tpr * rpb) % 32 == 0 and ms > 0
         G.fit_device(ctx, desc, data, None, None, *out)
         torch.cuda.synchronize()
         ref = O.fit(oracle_desc(O, w), w.data)
