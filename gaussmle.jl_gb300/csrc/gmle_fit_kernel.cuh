@@ -1854,11 +1854,12 @@ __global__ void __launch_bounds__(128) fit_kernel_r1(const KernelArgs a, const T
 // column's pixels, and whole columns of rows are independent work: a lane
 // alone on its scheduler is bound by these chains' latency, not by issue.
 //
-// Two lanes (measured at 10 000 XYNB 11x11 ROIs): with about one warp per
-// scheduler, a lane's time is its instruction count over the single-warp
-// issue rate, and two column blocks halve the pixel work while only the y
-// tables are evaluated twice.  Four lanes cut a lane's instructions further
-// but add 79 % to the ROI's total and share each scheduler between two warps.
+// Two column blocks evaluate only the y tables twice; four lanes cut a lane's
+// instructions further but add 79 % to the ROI's total (10 000 XYNB 11x11
+// ROIs: 127 k against 71 k lane instructions per ROI).  Measured at 10 000
+// ROIs: astigmatic 15x15 sCMOS 157 us with two lanes, 234 us with four; XYNB
+// 11x11 Poisson 77, 72 and 73 us with two, four and one, where a fit is
+// bound by the latency of its 21 dependent passes.
 template <int TPR> struct LaneGrid {
     static_assert(TPR == 2 || TPR == 4 || TPR == 8, "2, 4 or 8 lanes per ROI");
     static constexpr int NCX = TPR == 2 ? 2 : 4;
