@@ -26,6 +26,7 @@
 #include <chrono>
 #include <condition_variable>
 #include <cstdio>
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -718,24 +719,43 @@ gmle_status gmle_server_stop(gmle_ctx *ctx)
     return GMLE_OK;
 }
 
-gmle_status gmle_submit(gmle_ctx *ctx, const gmle_group *request, uint64_t *ticket)
+// Whether every corner of n ROIs of edge `box` lies inside an nx x ny map
+// (1-based): the smallest and largest corner along each axis, in a loop the
+// compiler vectorises, then the first offending ROI only if one exists.
+static int64_t first_bad_corner(const int32_t *xc, const int32_t *yc, int64_t n, int box,
+                                int32_t nx, int32_t ny)
 {
-    if (!ctx || !request || !ticket) return GMLE_INVALID_ARG;
-    Server *S = ctx->server;
-    if (!S) return fail(ctx, GMLE_INVALID_ARG, "server not started");
+    int32_t mnx = INT32_MAX, mny = INT32_MAX, mxx = INT32_MIN, mxy = INT32_MIN;
+    for (int64_t k = 0; k < n; k++) {
+        mnx = std::min(mnx, xc[k]);
+        mxx = std::max(mxx, xc[k]);
+        mny = std::min(mny, yc[k]);
+        mxy = std::max(mxy, yc[k]);
+    }
+    const auto bad = [&](int64_t x, int64_t y) {
+        return x < 1 || y < 1 || x + box - 1 > nx || y + box - 1 > ny;
+    };
+    if (n <= 0 || !(bad(mnx, mny) || bad(mxx, mxy))) return -1;
+    for (int64_t k = 0; k < n; k++)
+        if (bad(xc[k], yc[k])) return k;
+    return -1;
+}
+
+// gmle_submit without waking the scheduler (notify: whether to wake it).
+static gmle_status submit_one(gmle_ctx *ctx, Server *S, const gmle_group *request,
+                              uint64_t *ticket, bool notify)
+{
     {
         std::lock_guard<std::mutex> lk(ctx->mu);
         gmle_status st = validate_groups(ctx, request, 1);
         if (st != GMLE_OK) return st;
         if (request->n <= 0) return fail(ctx, GMLE_INVALID_ARG, "request without ROIs");
         if (request->desc.camera != GMLE_CAMERA_POISSON) {
-            const int64_t box = request->desc.box;
-            for (int64_t k = 0; k < request->n; k++) {
-                const int64_t x = request->x_corners[k], y = request->y_corners[k];
-                if (x < 1 || y < 1 || x + box - 1 > ctx->nx || y + box - 1 > ctx->ny)
-                    return fail(ctx, GMLE_INVALID_ARG,
-                                "ROI %lld: corner outside the calibration map", (long long)k);
-            }
+            const int64_t k = first_bad_corner(request->x_corners, request->y_corners,
+                                               request->n, request->desc.box, ctx->nx, ctx->ny);
+            if (k >= 0)
+                return fail(ctx, GMLE_INVALID_ARG,
+                            "ROI %lld: corner outside the calibration map", (long long)k);
         }
     }
     Request *r = new Request();
@@ -814,8 +834,34 @@ gmle_status gmle_submit(gmle_ctx *ctx, const gmle_group *request, uint64_t *tick
         }
         *ticket = r->ticket;
     }
-    S->cv_work.notify_one();
+    if (notify) S->cv_work.notify_one();
     return GMLE_OK;
+}
+
+gmle_status gmle_submit(gmle_ctx *ctx, const gmle_group *request, uint64_t *ticket)
+{
+    if (!ctx || !request || !ticket) return GMLE_INVALID_ARG;
+    Server *S = ctx->server;
+    if (!S) return fail(ctx, GMLE_INVALID_ARG, "server not started");
+    return submit_one(ctx, S, request, ticket, true);
+}
+
+gmle_status gmle_submit_many(gmle_ctx *ctx, const gmle_group *requests, int32_t n,
+                             uint64_t *tickets, int32_t *submitted)
+{
+    if (submitted) *submitted = 0;
+    if (!ctx || n < 0 || (n > 0 && (!requests || !tickets))) return GMLE_INVALID_ARG;
+    Server *S = ctx->server;
+    if (!S) return fail(ctx, GMLE_INVALID_ARG, "server not started");
+    gmle_status st = GMLE_OK;
+    int32_t k = 0;
+    for (; k < n; k++) {
+        st = submit_one(ctx, S, &requests[k], &tickets[k], false);
+        if (st != GMLE_OK) break;
+    }
+    if (submitted) *submitted = k;
+    if (k > 0) S->cv_work.notify_one();
+    return st;
 }
 
 static gmle_status finish_locked(Server *S, Request *r)

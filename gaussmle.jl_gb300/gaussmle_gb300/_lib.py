@@ -34,6 +34,7 @@ EXPORTED = [
     "gmle_set_calibration", "gmle_fit", "gmle_fit_device", "gmle_fit_device_errors",
     "gmle_get_tuning", "gmle_set_tuning", "gmle_autotune", "gmle_kernel_launches",
     "gmle_fit_mixed_device", "gmle_server_start", "gmle_server_stop", "gmle_submit",
+    "gmle_submit_many",
     "gmle_poll", "gmle_wait", "gmle_server_stats_get", "gmle_fit_mixed_device_noalloc",
     "gmle_pvalues", "gmle_pvalues_device", "gmle_cut_rois_device", "gmle_simulate_device",
     "gmle_math_selftest",
@@ -130,6 +131,8 @@ def load(path: str | Path | None = None) -> C.CDLL:
             "gmle_server_start": ([vp, C.POINTER(ServerConfig)], C.c_int),
             "gmle_server_stop": ([vp], C.c_int),
             "gmle_submit": ([vp, C.POINTER(Group), C.POINTER(C.c_uint64)], C.c_int),
+            "gmle_submit_many": ([vp, C.POINTER(Group), C.c_int32, C.POINTER(C.c_uint64),
+                                  C.POINTER(C.c_int32)], C.c_int),
             "gmle_poll": ([vp, C.c_uint64], C.c_int),
             "gmle_wait": ([vp, C.c_uint64, i64], C.c_int),
             "gmle_server_stats_get": ([vp, C.POINTER(ServerStats), i32], C.c_int),

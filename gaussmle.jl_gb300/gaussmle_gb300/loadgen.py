@@ -67,6 +67,12 @@ class HostPools:
         return G
 
 
+def group_array(pools: HostPools, reqs: list[Request]):
+    """The requests' descriptors as one ctypes array of Group (for
+    Server.submit_many)."""
+    return (_lib.Group * len(reqs))(*[pools.group_struct(r) for r in reqs])
+
+
 def make_stream(pools: HostPools, total_rois: int, seed: int = 7, lo: int = 50,
                 hi: int = 50000) -> list[Request]:
     """Requests until total_rois: sizes log-uniform [lo, hi] (all `lo` when
@@ -88,15 +94,20 @@ def make_stream(pools: HostPools, total_rois: int, seed: int = 7, lo: int = 50,
     return out
 
 
-def run_batch_served(srv: Server, pools: HostPools, reqs: list[Request]) -> float:
+def run_batch_served(srv: Server, pools: HostPools, reqs: list[Request], groups=None) -> float:
     """Submit every request at once, wait for all; returns seconds (Python's
-    cyclic collector paused meanwhile)."""
+    cyclic collector paused meanwhile).  With `groups` (group_array(reqs),
+    descriptors built beforehand, as a client holds them) the requests go in
+    one gmle_submit_many call; without, one gmle_submit each."""
     import gc
     gc_was = gc.isenabled()
     gc.disable()
     try:
         t0 = time.perf_counter()
-        tickets = [srv.submit(pools.group_struct(r)) for r in reqs]
+        if groups is not None:
+            tickets = srv.submit_many(groups)
+        else:
+            tickets = [srv.submit(pools.group_struct(r)) for r in reqs]
         for t in tickets:
             srv.wait(t)
         return time.perf_counter() - t0

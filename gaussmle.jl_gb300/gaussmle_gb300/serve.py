@@ -72,6 +72,22 @@ class Server:
         self._keep[t.value] = (group, keep)
         return t.value
 
+    def submit_many(self, groups, keep=()) -> list[int]:
+        """Submit requests in one call (gmle_submit_many): `groups` is a ctypes
+        array of Group (or a list, copied into one).  Returns their tickets;
+        raises on the first request not accepted (the ones before it stay
+        submitted and their tickets are kept for wait())."""
+        n = len(groups)
+        arr = groups if isinstance(groups, C.Array) else (_lib.Group * n)(*groups)
+        tk = (C.c_uint64 * n)()
+        done = C.c_int32()
+        st = self.ctx.lib.gmle_submit_many(self.ctx.handle, arr, n, tk, C.byref(done))
+        out = list(tk[: done.value])
+        for k, t in enumerate(out):
+            self._keep[t] = (arr, keep)
+        self.ctx.check(st)
+        return out
+
     def wait(self, ticket: int, timeout_s: float | None = None) -> None:
         ns = -1 if timeout_s is None else int(timeout_s * 1e9)
         st = self.ctx.lib.gmle_wait(self.ctx.handle, ticket, ns)

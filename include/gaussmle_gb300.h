@@ -382,6 +382,12 @@ gmle_status gmle_server_stop(gmle_ctx *ctx);
 /* Queue one request (host pointers, flags may be NULL).  GMLE_ADMISSION_REJECTED
  * when it can never fit the arena or the queue is full. */
 gmle_status gmle_submit(gmle_ctx *ctx, const gmle_group *request, uint64_t *ticket);
+/* gmle_submit of n requests in order, in one call: tickets[k] is request k's.
+ * Stops at the first request that is not accepted and returns its status;
+ * *submitted (may be NULL) is the number accepted before it.  The scheduler
+ * is woken once, after the last. */
+gmle_status gmle_submit_many(gmle_ctx *ctx, const gmle_group *requests, int32_t n,
+                             uint64_t *tickets, int32_t *submitted);
 /* GMLE_OK when the request is done (its outputs are written), GMLE_NOT_READY
  * while it runs, or the status it failed with.  A finished ticket is
  * forgotten once GMLE_OK (or its failure) has been returned. */

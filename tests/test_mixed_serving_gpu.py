@@ -7,6 +7,8 @@
   FP32 oracle within the parity bar (tests/parity_cases.py).
 * Admission: a request that can never fit the HBM budget is rejected;
   requests beyond the free budget queue and complete.
+* gmle_submit_many gives the results of one gmle_submit per request and
+  stops at the first request it does not accept.
 """
 import ctypes as C
 
@@ -14,7 +16,7 @@ import numpy as np
 import pytest
 
 import gaussmle_gb300 as G
-from gaussmle_gb300 import serve
+from gaussmle_gb300 import _lib, serve
 from gaussmle_gb300.fitter import make_desc
 from oracle import oracle as O
 from parity_cases import compare, make_case, oracle_desc
@@ -284,3 +286,42 @@ def test_many_requests_from_threads(ctx, graphs, pinned):
     for (lo, hi), b in zip(slices, outs):
         for key in ("params", "crlb", "llr", "flags"):
             assert np.array_equal(b[key], whole[key][lo:hi], equal_nan=True), (lo, hi, key)
+
+
+def test_submit_many_matches_one_at_a_time_and_stops_at_a_bad_request(ctx):
+    """gmle_submit_many: the same results as one gmle_submit per request; a
+    request with a corner outside the map stops it there (GMLE_INVALID_ARG)
+    with the requests before it submitted and served."""
+    ws = _cases()
+    _set_maps(ctx, ws[0].maps)
+    srv = serve.Server(ctx, hbm_budget_bytes=256 << 20)
+    try:
+        one = []
+        for w in ws:
+            b = _host_bufs(w)
+            srv.wait(srv.submit(_group(w, b), keep=b), timeout_s=60)
+            one.append(b)
+        bufs = [_host_bufs(w) for w in ws]
+        tickets = srv.submit_many([_group(w, b) for w, b in zip(ws, bufs)], keep=bufs)
+        assert len(tickets) == len(ws)
+        for t in tickets:
+            srv.wait(t, timeout_s=120)
+        for w, a, b in zip(ws, one, bufs):
+            for key in ("params", "crlb", "llr", "flags"):
+                assert np.array_equal(a[key], b[key], equal_nan=True), (w.name, key)
+        # the second request has one corner past the map's edge
+        bufs = [_host_bufs(w) for w in ws[:3]]
+        bufs[1]["xc"] = bufs[1]["xc"].copy()
+        bufs[1]["xc"][min(5, ws[1].n - 1)] = max(ws[1].maps[0].shape) + 1
+        groups = [_group(w, b) for w, b in zip(ws[:3], bufs)]
+        arr = (_lib.Group * 3)(*groups)
+        tk = (C.c_uint64 * 3)()
+        done = C.c_int32(-1)
+        st = ctx.lib.gmle_submit_many(ctx.handle, arr, 3, tk, C.byref(done))
+        assert st == 1 and done.value == 1  # GMLE_INVALID_ARG at request 1
+        assert b"corner outside the calibration map" in ctx.lib.gmle_last_error(ctx.handle)
+        assert ctx.lib.gmle_wait(ctx.handle, tk[0], int(60e9)) == 0
+        for key in ("params", "crlb", "llr", "flags"):
+            assert np.array_equal(bufs[0][key], one[0][key], equal_nan=True), key
+    finally:
+        srv.stop()
