@@ -668,10 +668,13 @@ __device__ __forceinline__ void cp_async4(void *dst, const void *src, unsigned s
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(src),
                  "r"(src_bytes) : "memory");
 }
+// .ca, not .cg: from pinned host memory (ROI data the serving loop reads in
+// place) 16-byte .cg copies ran at 93 GB/s on GB300, .ca copies, 4-byte
+// copies and plain loads at the host link's 211 GB/s; from HBM they are alike.
 __device__ __forceinline__ void cp_async16(void *dst, const void *src)
 {
     const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(src) : "memory");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all()
 {
