@@ -140,4 +140,64 @@ function pvalues(log_likelihoods::Vector{Float32}, box::Integer, nparams::Intege
     return pv
 end
 
+# ---- serving loop (gmle_server_* / gmle_submit* / gmle_wait) ------------------
+
+# gmle_group: one request; host pointers for gmle_submit / gmle_submit_many
+struct GmleGroup
+    desc::FitDesc
+    data::Ptr{Float32}
+    x_corners::Ptr{Int32}
+    y_corners::Ptr{Int32}
+    n::Int64
+    params::Ptr{Float32}
+    crlb::Ptr{Float32}
+    llr::Ptr{Float32}
+    flags::Ptr{UInt8}
+end
+
+# gmle_server_config (zeros: the defaults)
+struct ServerConfig
+    hbm_budget_bytes::Int64
+    max_inflight_steps::Int32
+    max_step_rois::Int64
+    max_pending::Int32
+    use_graphs::Int32
+end
+
+function server_start!(ctx::Context; hbm_budget_bytes = 0, max_inflight_steps = 0,
+                       max_step_rois = 0, max_pending = 0, use_graphs = false)
+    cfg = Ref(ServerConfig(hbm_budget_bytes, max_inflight_steps, max_step_rois, max_pending,
+                           Int32(use_graphs)))
+    check(ctx, ccall((:gmle_server_start, libgmle), Cint, (Ptr{Cvoid}, Ref{ServerConfig}),
+                     ctx.ptr, cfg))
+end
+
+server_stop!(ctx::Context) = check(ctx, ccall((:gmle_server_stop, libgmle), Cint,
+                                              (Ptr{Cvoid},), ctx.ptr))
+
+"""
+    submit!(ctx, requests) -> tickets
+
+Queues `requests` (a `Vector{GmleGroup}` whose host arrays the caller keeps
+alive until each ticket is waited for) in one `gmle_submit_many` call.
+"""
+function submit!(ctx::Context, requests::Vector{GmleGroup})
+    tickets = Vector{UInt64}(undef, length(requests))
+    accepted = Ref{Int32}(0)
+    st = ccall((:gmle_submit_many, libgmle), Cint,
+               (Ptr{Cvoid}, Ptr{GmleGroup}, Int32, Ptr{UInt64}, Ref{Int32}),
+               ctx.ptr, requests, Int32(length(requests)), tickets, accepted)
+    check(ctx, st)
+    return tickets
+end
+
+"""
+    wait!(ctx, ticket; timeout_ns = -1)
+
+Blocks until the request is done (its outputs written) or fails.
+"""
+wait!(ctx::Context, ticket::UInt64; timeout_ns::Integer = -1) =
+    check(ctx, ccall((:gmle_wait, libgmle), Cint, (Ptr{Cvoid}, UInt64, Int64), ctx.ptr, ticket,
+                     Int64(timeout_ns)))
+
 end # module
