@@ -733,8 +733,8 @@ def run_ours(args):
         torch.cuda.empty_cache()
         ext = extras(torch, ctx, dev, max(3, args.steps // 2), peak_inst)
     if e2e is not None and plain is not None:
-        # the spec comparison: the served form against the reference's
-        # one-call-per-batch pattern on the same requests
+        # the served form against the reference's one-call-per-batch pattern
+        # on the same requests
         e2e["served_over_plain"] = e2e["value"] / plain["per_request_gmle_fit"]["value"]
         e2e["plain_per_request_fits_per_s"] = plain["per_request_gmle_fit"]["value"]
     if e2e is not None and latency is not None:

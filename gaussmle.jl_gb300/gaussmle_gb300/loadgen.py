@@ -50,21 +50,18 @@ class HostPools:
             })
         frac = np.array([gr["n"] for gr in groups], float)
         self.p = frac / frac.sum()
+        # per group: its fit descriptor (the same for every request of the
+        # group, as a client holds it) and its buffers' base addresses
+        self.desc = [make_desc(gr["psf"], gr["box"], 20, gr["constraints"], gr["camera"])
+                     for gr in groups]
+        self.base = [{k: h[k].data_ptr() for k in h} for h in self.h]
 
     def group_struct(self, r: Request) -> _lib.Group:
-        gr, h = self.g[r.group], self.h[r.group]
+        gr, b = self.g[r.group], self.base[r.group]
         b2, P = gr["box"] * gr["box"], gr["psf"].nparams
-        G = _lib.Group()
-        G.desc = make_desc(gr["psf"], gr["box"], 20, gr["constraints"], gr["camera"])
-        G.data = C.c_void_p(h["data"].data_ptr() + 4 * b2 * r.lo)
-        G.x_corners = C.c_void_p(h["xc"].data_ptr() + 4 * r.lo)
-        G.y_corners = C.c_void_p(h["yc"].data_ptr() + 4 * r.lo)
-        G.n = r.n
-        G.params = C.c_void_p(h["params"].data_ptr() + 4 * P * r.lo)
-        G.crlb = C.c_void_p(h["crlb"].data_ptr() + 4 * P * r.lo)
-        G.llr = C.c_void_p(h["llr"].data_ptr() + 4 * r.lo)
-        G.flags = C.c_void_p(h["flags"].data_ptr() + r.lo)
-        return G
+        return _lib.Group(self.desc[r.group], b["data"] + 4 * b2 * r.lo, b["xc"] + 4 * r.lo,
+                          b["yc"] + 4 * r.lo, r.n, b["params"] + 4 * P * r.lo,
+                          b["crlb"] + 4 * P * r.lo, b["llr"] + 4 * r.lo, b["flags"] + r.lo)
 
 
 def group_array(pools: HostPools, reqs: list[Request]):
