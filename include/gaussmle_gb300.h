@@ -385,7 +385,8 @@ gmle_status gmle_submit(gmle_ctx *ctx, const gmle_group *request, uint64_t *tick
 /* gmle_submit of n requests in order, in one call: tickets[k] is request k's.
  * Stops at the first request that is not accepted and returns its status;
  * *submitted (may be NULL) is the number accepted before it.  The scheduler
- * is woken once, after the last. */
+ * is woken after the first request and every 16th, so that the first steps
+ * start while later requests are still being queued. */
 gmle_status gmle_submit_many(gmle_ctx *ctx, const gmle_group *requests, int32_t n,
                              uint64_t *tickets, int32_t *submitted);
 /* GMLE_OK when the request is done (its outputs are written), GMLE_NOT_READY
