@@ -379,6 +379,27 @@ def parity_report(run, outs, gpu_out, groups, n_fp64: int = 3000) -> dict:
     return rep
 
 
+def host_cpu() -> str:
+    """The host CPU's model and core count (/proc/cpuinfo, else platform)."""
+    import platform
+    name = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            info = f.read()
+        for key in ("model name", "Model Name", "CPU part"):
+            for line in info.splitlines():
+                if line.startswith(key):
+                    name = line.split(":", 1)[1].strip()
+                    break
+            if name:
+                break
+        if name and name.lower().startswith("0xd4f"):  # Arm CPU part number
+            name = "Arm Neoverse-V2"
+    except OSError:
+        pass
+    return f"{name or platform.processor() or platform.machine()}, {os.cpu_count()} cores"
+
+
 def cpu_baseline(groups, maps, seconds: float, gpu_out=None) -> dict:
     run, m, nth = oracle_sample(groups, maps, 4000, 0)
     t0 = time.perf_counter()
@@ -389,7 +410,7 @@ def cpu_baseline(groups, maps, seconds: float, gpu_out=None) -> dict:
     t = time.perf_counter()
     outs = run()
     t = time.perf_counter() - t
-    out = {"value": m / t, "unit": UNIT, "cores": nth, "kind": "port",
+    out = {"value": m / t, "unit": UNIT, "cores": nth, "kind": "port", "cpu": host_cpu(),
            "sample": f"{m} ROIs of the mixed batch, in its proportions (the first ROIs of each "
                      f"group; {t:.1f} s on {nth} host threads; FP32 restatement of the "
                      "reference CPU path, oracle/gmle_oracle.c)"}
@@ -425,7 +446,7 @@ def run_reference(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "rois_per_step": m, "iterations": 20},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nth, "kind": "port",
-                         "sample": sample},
+                         "cpu": host_cpu(), "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
 
