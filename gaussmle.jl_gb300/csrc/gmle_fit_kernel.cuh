@@ -1057,12 +1057,19 @@ __device__ __forceinline__ bool stage_r1(const KernelArgs &a, float *spix, int64
         for (int e = cnt + l; e < 32 * B2; e += 32) wpix[e] = 0.f;
         cp_async_wait_all();
         __syncwarp();
-        // ADU -> e-, two ROIs (2 NJP gathers of each map) in flight at a time
+        // ADU -> e-, H ROIs (2 H NJP gathers of the maps) in flight at a time.
+        // The conversion's dependent rounds of L2 gathers were 63 % of the
+        // staging of a 15x15 block (clock64 per phase: 40.6 k of 64.7 k cycles;
+        // staging 14 % of a block's life).  Measured, 300 000 ROIs: 15x15
+        // with H = 4 1.824 -> 1.755 ms (H = 8: 1.808); 13x13 slower with more
+        // (1.326 ms at H = 2, 1.344 at 4, 1.366 at 8): the fit's schedule
+        // shifts with the registers the staging holds.
         if (a.adu) {
-            for (int r = 0; r < nw; r += 2) {
-                float off[2][NJP], gn[2][NJP];
+            constexpr int H = BOX >= 15 ? 4 : 2;
+            for (int r = 0; r < nw; r += H) {
+                float off[H][NJP], gn[H][NJP];
 #pragma unroll
-                for (int h = 0; h < 2; h++) {
+                for (int h = 0; h < H; h++) {
                     // lanes past the warp's ROIs hold ok == false
                     const long long b = __shfl_sync(0xffffffffu, base, (r + h) & 31);
                     const bool okr = __shfl_sync(0xffffffffu, ok, (r + h) & 31) && r + h < 32;
@@ -1079,7 +1086,7 @@ __device__ __forceinline__ bool stage_r1(const KernelArgs &a, float *spix, int64
                     }
                 }
 #pragma unroll
-                for (int h = 0; h < 2; h++) {
+                for (int h = 0; h < H; h++) {
                     if (r + h >= nw) break;
 #pragma unroll
                     for (int jp = 0; jp < NJP; jp++) {
