@@ -54,8 +54,8 @@ WORKLOAD = ("mixed-batch: 40% XYNB 11x11, 25% XYNBS 9x9, 15% XYNBSXSY 13x13, "
 # captured launch); the roofline's traffic scales it to the timed launch.
 TRAFFIC_BYTES_PER_ROI: dict[str, float] = {
     # 90 000 ROIs, one thread per ROI, 128 ROIs/block (variances in tensor
-    # memory, per-warp staging): 168.3 MB read + 5.3 MB written
-    "fit_kernel_r1<3, 15, true, false>": 1929.1,
+    # memory, per-warp staging): 168.8 MB read + 4.8 MB written
+    "fit_kernel_r1<3, 15, true, false>": 1928.0,
     # 240 000 ROIs, one thread per ROI, 128 ROIs/block (variances in tensor
     # memory): 199.4 MB read + 8.9 MB written
     "fit_kernel_r1<0, 11, true, false>": 867.9,
