@@ -1587,7 +1587,6 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
     using S = Slots<MODEL>;
     static_assert(B2 >= P, "a warp's pixel slots stage its results");
 
-    const int R = blockDim.x;
     float *spix = smem;
     const bool valid = stage_r1<BOX, SCMOS>(a, spix, roi0, nroi, taddr);
 
@@ -1812,8 +1811,20 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
 // sCMOS: warp 0 allocates the CTA's tensor memory for the variance tiles before
 // the first tile and frees it after the last; no path leaves the kernel
 // between the two.
+//
+// Residency: XYNBS 9x9 sCMOS asks for four blocks per SM (128 registers; its
+// shared memory would allow five and its tensor memory four), where its 163
+// registers gave three: 500 000 ROIs 1.060 -> 0.990 ms, the mixed batch
+// 343.6 -> 348.0 M fits/s (the table kernel spills 76 bytes and runs as
+// before).  Every other kernel passes 0, i.e. no minimum: an explicit 1 lets
+// the compiler take up to 255 registers (XYNB 11x11 sCMOS: 251 instead of
+// 142, two blocks per SM instead of three).
+template <int MODEL, int BOX, bool SCMOS>
+constexpr int r1_min_blocks() { return (MODEL == 1 && BOX == 9 && SCMOS) ? 4 : 0; }
+
 template <int MODEL, int BOX, bool SCMOS, bool TABLE, bool LM = false>
-__global__ void __launch_bounds__(128) fit_kernel_r1(const KernelArgs a, const TileTable t)
+__global__ void __launch_bounds__(128, (LM ? 0 : r1_min_blocks<MODEL, BOX, SCMOS>()))
+    fit_kernel_r1(const KernelArgs a, const TileTable t)
 {
     extern __shared__ __align__(16) float smem[];
     __shared__ uint32_t s_tmem;
