@@ -136,6 +136,16 @@ __device__ __forceinline__ float ex2_approx(float x)
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 }
+// ln(x) = log2(x) * ln 2 (PTX lg2.approx, subnormal inputs kept: about 2^-22
+// absolute in log2, i.e. within a few ulp of ln for the photon counts and
+// model values the Poisson LLR takes; the library's logf costs 26 issued
+// instructions, and the final pass takes two per pixel)
+__device__ __forceinline__ float log_approx(float x)
+{
+    float r;
+    asm("lg2.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r * 0.69314718055994531f;
+}
 // exp(-t^2 / 2) = 2^(t^2 * (-log2(e) / 2)); the rounding of the exponent
 // costs at most |t^2| 2^-23 relative, i.e. nothing where the value matters.
 __device__ __forceinline__ float gauss_edge(float t)
@@ -1287,16 +1297,22 @@ __device__ __forceinline__ float qsym(const float (&Q)[NB][NB], int p, int q)
 // Per pixel of the final pass: the LLR term (compute_log_likelihood,
 // src/camera_models.jl:60-96) and the Fisher weight sums Q_pq += b_p b_q w,
 // w = 1/variance over pixels with mu > 0 (src/unified_kernel.jl:378-396).
-template <bool SCMOS, bool SIG, int NB>
+// FAST_LOG: the Poisson LLR's logarithms by log_approx (the final pass, whose
+// LLR is an output only); the full-Hessian passes, which accept or reject a
+// step on the LLR, keep the library's logf.
+template <bool SCMOS, bool SIG, int NB, bool FAST_LOG = true>
 __device__ __forceinline__ void final_pixel(float d, float v, float mu, float py, float yd1,
                                             float ys1, float &llr, float (&Q)[NB][NB])
 {
     const float rv = rcp_approx(SCMOS ? mu + v : mu);
     if (!SCMOS) {
-        if (mu > 0.f && d > 0.f)
-            llr += d * logf(mu) - mu - (d * logf(d) - d);
-        else if (mu > 0.f && d == 0.f)
+        if (mu > 0.f && d > 0.f) {
+            const float lm = FAST_LOG ? log_approx(mu) : logf(mu);
+            const float ld = FAST_LOG ? log_approx(d) : logf(d);
+            llr += d * lm - mu - (d * ld - d);
+        } else if (mu > 0.f && d == 0.f) {
             llr -= mu;
+        }
     } else {
         const float tv = mu + v;
         if (tv > 0.f) {
@@ -1377,7 +1393,7 @@ __device__ __forceinline__ void lm_pixel(float d, float v, float mu, float py, f
                                          float ys1, float &llr, float (&Q)[NB][NB],
                                          float (&Rs)[NB])
 {
-    final_pixel<SCMOS, SIG, NB>(d, v, mu, py, yd1, ys1, llr, Q);
+    final_pixel<SCMOS, SIG, NB, false>(d, v, mu, py, yd1, ys1, llr, Q);
     float cf, df;
     likelihood_terms<SCMOS>(d, v, mu, cf, df);
     Rs[0] = fmaf(py, cf, Rs[0]);

@@ -1,10 +1,11 @@
 // gmle_math.cu - the fit kernels' own elementary functions, evaluated for
 // a check of their accuracy (gmle_math_selftest).
 //
-// The fit evaluates erf and exp at every pixel edge of every iteration and a
-// reciprocal at every pixel (gmle_fit_kernel.cuh: erf_from_gauss, gauss_edge,
-// rcp_approx).  This entry point evaluates them on caller-supplied arguments
-// next to the CUDA library's erff, expf and IEEE division, in the same
+// The fit evaluates erf and exp at every pixel edge of every iteration, a
+// reciprocal at every pixel and, in the Poisson final pass, two logarithms per
+// pixel (gmle_fit_kernel.cuh: erf_from_gauss, gauss_edge, rcp_approx,
+// log_approx).  This entry point evaluates them on caller-supplied arguments
+// next to the CUDA library's erff, expf, IEEE division and logf, in the same
 // kernel, so that a test can bound their error against those and against an
 // FP64 reference on the host.
 #include <cuda_runtime.h>
@@ -28,6 +29,9 @@ __global__ void math_selftest_kernel(const float *__restrict__ x, int64_t n, flo
     out[3 * n + i] = expf(-0.5f * (v * v));
     out[4 * n + i] = gmle::rcp_approx(v);
     out[5 * n + i] = __fdiv_rn(1.0f, v);
+    // the Poisson LLR's logarithm at |x| (its arguments are positive)
+    out[6 * n + i] = gmle::log_approx(fabsf(v));
+    out[7 * n + i] = logf(fabsf(v));
 }
 
 }  // namespace

@@ -244,10 +244,11 @@ gmle_status gmle_pvalues_device(gmle_ctx *ctx, const float *d_llr, int64_t n, in
 /*
  * Accuracy check of the fit kernels' own elementary functions (no reference
  * counterpart: the reference calls SpecialFunctions.erf and Base.exp).  For
- * each of the n device-resident arguments x[i], writes into d_out ((6, n),
+ * each of the n device-resident arguments x[i], writes into d_out ((8, n),
  * row k at d_out + k n): 0 the fit's erf(x) (from exp(-x^2) at the same
  * edge), 1 the CUDA library's erff(x), 2 the fit's exp(-x^2 / 2), 3 expf of
- * the same, 4 the fit's 1/x, 5 the IEEE 1/x.  Enqueued on `stream`.
+ * the same, 4 the fit's 1/x, 5 the IEEE 1/x, 6 the fit's ln|x|, 7 logf(|x|).
+ * Enqueued on `stream`.
  */
 gmle_status gmle_math_selftest(const float *d_x, int64_t n, float *d_out, void *stream);
 

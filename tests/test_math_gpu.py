@@ -2,14 +2,17 @@
 
 The fit evaluates erf and exp once per pixel edge and a reciprocal once per
 pixel (gmle_fit_kernel.cuh: erf_from_gauss, gauss_edge, rcp_approx) instead of
-the library's erff (28 issued instructions), expf (9) and __fdividef (4).
-Bounds checked here, on a dense grid and at the pixel-edge arguments of the
-fits (|x| up to 8 pixel sigmas):
+the library's erff (28 issued instructions), expf (9) and __fdividef (4), and
+the Poisson final pass's two logarithms per pixel by log_approx instead of
+logf (26).  Bounds checked here, on a dense grid and at the pixel-edge
+arguments of the fits (|x| up to 8 pixel sigmas):
   * erf: within 5e-7 absolute of the FP64 erf (measured 4.3e-7, near x = 0;
     erff: 6e-8), within 6e-7 of erff;
   * exp(-x^2/2): within 4 ulp plus 6e-8 x^2 relative (the exponent's
     rounding) where above 1e-30;
-  * 1/x: within 1 ulp of the IEEE quotient.
+  * 1/x: within 1 ulp of the IEEE quotient;
+  * ln x (photon counts and model values, 1e-6 to 1e7, and subnormals):
+    within 3e-7 absolute plus 2 ulp of the FP64 logarithm.
 """
 import ctypes as C
 
@@ -24,7 +27,7 @@ def run(ctx, x):
     torch = pytest.importorskip("torch")
     dev = torch.device("cuda", 0)
     xd = torch.from_numpy(np.ascontiguousarray(x, np.float32)).to(dev)
-    out = torch.empty((6, len(x)), device=dev)
+    out = torch.empty((8, len(x)), device=dev)
     ctx.check(ctx.lib.gmle_math_selftest(C.c_void_p(xd.data_ptr()), len(x),
                                          C.c_void_p(out.data_ptr()), None))
     torch.cuda.synchronize()
@@ -67,3 +70,17 @@ def test_erf_is_monotone_and_odd(ctx):
     assert np.array_equal(pos, -neg)
     # increasing up to rounding: no step back larger than 2 ulp of 1
     assert np.diff(pos).min() >= -2.5e-7
+
+
+def test_log_accuracy(ctx):
+    rng = np.random.default_rng(5)
+    x = np.concatenate([np.geomspace(1e-6, 1e7, 400_001), rng.uniform(0.5, 2e4, 200_000),
+                        np.arange(1, 20_001), [1e-40, 1e-44, 3e38]]).astype(np.float32)
+    o = run(ctx, x)
+    ref = np.log(x.astype(np.float64))
+    err = np.abs(o[6] - ref)
+    lib = np.abs(o[7] - ref)
+    ulp = np.spacing(np.abs(ref).astype(np.float32)).astype(np.float64)
+    print(f"\nln: fit max |err| {err.max():.3e} (max in ulp {(err / ulp).max():.2f}), "
+          f"logf max |err| {lib.max():.3e}")
+    assert np.all(err <= 3e-7 + 2 * ulp)
