@@ -1205,6 +1205,41 @@ __device__ __forceinline__ bool uncapped(float N, float bg, float dmax)
     return bg > 0.01f && N >= 0.f && dmax <= 9900.f * fminf(bg, bg * bg);
 }
 
+// ---- two pixels at once: packed FP32 pairs ------------------------------------
+//
+// sm_100's add/mul/fma .f32x2 take one issue slot for two FP32 operations, each
+// half rounded exactly like the scalar operation.  The one-thread kernel's
+// Newton pixel loop runs rows (t, t+1) of a column as one pair.  Each half
+// evaluates likelihood_terms / _uncapped's expressions with every operation
+// rounded as written, none contracted into an FMA (d - mu as fma(mu, -1, d):
+// one rounding, like the subtraction), as the reference evaluates them.
+__device__ __forceinline__ float2 f2(float x) { return make_float2(x, x); }
+
+template <bool SCMOS, bool UNCAPPED>
+__device__ __forceinline__ void likelihood_terms2(float2 d, float2 v, float2 mu, float2 &cf,
+                                                  float2 &df)
+{
+    if constexpr (SCMOS) {
+        const float2 s = __fadd2_rn(mu, v);
+        const float2 rv = make_float2(rcp_approx(s.x), rcp_approx(s.y));
+        cf = __fmul2_rn(__ffma2_rn(mu, f2(-1.0f), d), rv);
+        df = rv;
+    } else {
+        const float2 rm = make_float2(rcp_approx(mu.x), rcp_approx(mu.y));
+        const float2 q = __fmul2_rn(d, rm);
+        const float2 c = __fadd2_rn(q, f2(-1.0f));
+        const float2 e = __fmul2_rn(q, rm);
+        if constexpr (UNCAPPED) {
+            cf = c;
+            df = e;
+        } else {
+            const bool p0 = mu.x > 0.01f, p1 = mu.y > 0.01f;
+            cf = make_float2(p0 ? fminf(c.x, 1e4f) : 0.f, p1 ? fminf(c.y, 1e4f) : 0.f);
+            df = make_float2(p0 ? fminf(e.x, 1e4f) : 0.f, p1 ? fminf(e.y, 1e4f) : 0.f);
+        }
+    }
+}
+
 // Column-side contributions to gradient gs and diagonal Hessian hs of one pixel
 // column j with x-table entry (xp, xd1, xd2, xs1, xs2) and the column sums
 // A = sum_i py cf, B = sum_i py^2 df, E = sum_i cf, F = sum_i df,
@@ -1695,14 +1730,24 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
             }
             if constexpr (LM) lm_update<P>(th, thb, stp, gb, Fb, Lb, lam, it == 0, llr, gs, F);
         } else if (!final_pass) {
-            float py2[BOX], aG[CROSS ? BOX : 1], C[BOX], D[BOX];
+            // rows (2k, 2k + 1) as packed pairs (likelihood_terms2); an odd
+            // box's last row (even: the first partial sums) runs alone
+            constexpr int NPR = BOX / 2;
+            constexpr bool ODD = (BOX & 1) != 0;
+            float2 pyP[NPR], py2P[NPR], aGP[CROSS ? NPR : 1], CP[NPR], DP[NPR];
 #pragma unroll
-            for (int t = 0; t < BOX; t++) {
-                py2[t] = py[t] * py[t];
-                if (CROSS) aG[t] = py[t] * ys1[t];
-                C[t] = 0.f;
-                D[t] = 0.f;
+            for (int k = 0; k < NPR; k++) {
+                pyP[k] = make_float2(py[2 * k], py[2 * k + 1]);
+                py2P[k] = __fmul2_rn(pyP[k], pyP[k]);
+                if (CROSS) aGP[k] = make_float2(py[2 * k] * ys1[2 * k],
+                                                py[2 * k + 1] * ys1[2 * k + 1]);
+                CP[k] = f2(0.f);
+                DP[k] = f2(0.f);
             }
+            const float pyl = py[BOX - 1], py2l = pyl * pyl;
+            const float aGl = CROSS ? pyl * ys1[BOX - 1] : 0.f;
+            float Cl = 0.f, Dl = 0.f;
+            const float2 Nv = f2(N), bgv = f2(bg);
             float gs[P], hs[P];
 #pragma unroll
             for (int k = 0; k < P; k++) { gs[k] = 0.f; hs[k] = 0.f; }
@@ -1724,34 +1769,48 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
                     // next column's table entry: independent of this column's pixels
                     float nxp, nxd1, nxd2, nxs1 = 0.f, nxs2 = 0.f;
                     walk_entry<SIG, true, VOTE>(j + 1, ax, wx, nxp, nxd1, nxd2, nxs1, nxs2);
-                    const float npx = N * xp, xp2 = xp * xp;
+                    const float2 xpv = f2(xp);
+                    const float2 npx = __fmul2_rn(Nv, xpv), xp2 = __fmul2_rn(xpv, xpv);
                     const float *col = pix + (j - 1) * BOX * PS;
                     float nv[LW];
                     if (PIPE && j < BOX) tmem_ld_start<LW>(taddr + BOX * j, nv);
                     if (SCMOS && !PIPE) tmem_ld<LW>(taddr + BOX * (j - 1), vv);
-                    // even and odd rows in separate partial sums: two independent
-                    // FMA chains of box/2 instead of one of box
-                    float A[2] = {0.f, 0.f}, B[2] = {0.f, 0.f}, E[2] = {0.f, 0.f},
-                          F[2] = {0.f, 0.f}, Gc[2] = {0.f, 0.f};
+                    // even and odd rows in separate partial sums (.x, .y): two
+                    // independent FMA chains of box/2 instead of one of box
+                    float2 A = f2(0.f), B = f2(0.f), E = f2(0.f), F = f2(0.f), Gc = f2(0.f);
 #pragma unroll
-                    for (int t = 0; t < BOX; t++) {
-                        const float d = col[t];
-                        const float v = SCMOS ? vv[t] : 0.f;
-                        const float mu = fmaf(npx, py[t], bg);
+                    for (int k = 0; k < NPR; k++) {
+                        const int t = 2 * k;
+                        const float2 d = make_float2(col[t], col[t + 1]);
+                        const float2 v = SCMOS ? make_float2(vv[t], vv[t + 1]) : f2(0.f);
+                        const float2 mu = __ffma2_rn(npx, pyP[k], bgv);
+                        float2 cf, df;
+                        likelihood_terms2<SCMOS, UNCAPPED>(d, v, mu, cf, df);
+                        A = __ffma2_rn(pyP[k], cf, A);
+                        B = __ffma2_rn(py2P[k], df, B);
+                        E = __fadd2_rn(E, cf);
+                        F = __fadd2_rn(F, df);
+                        CP[k] = __ffma2_rn(xpv, cf, CP[k]);
+                        DP[k] = __ffma2_rn(xp2, df, DP[k]);
+                        if (CROSS) Gc = __ffma2_rn(aGP[k], df, Gc);
+                    }
+                    if constexpr (ODD) {
+                        const float d = col[BOX - 1];
+                        const float v = SCMOS ? vv[BOX - 1] : 0.f;
+                        const float mu = fmaf(npx.x, pyl, bg);
                         float cf, df;
                         if constexpr (UNCAPPED) likelihood_terms_uncapped(d, mu, cf, df);
                         else likelihood_terms<SCMOS>(d, v, mu, cf, df);
-                        const int h = t & 1;
-                        A[h] = fmaf(py[t], cf, A[h]);
-                        B[h] = fmaf(py2[t], df, B[h]);
-                        E[h] += cf;
-                        F[h] += df;
-                        C[t] = fmaf(xp, cf, C[t]);
-                        D[t] = fmaf(xp2, df, D[t]);
-                        if (CROSS) Gc[h] = fmaf(aG[t], df, Gc[h]);
+                        A.x = fmaf(pyl, cf, A.x);
+                        B.x = fmaf(py2l, df, B.x);
+                        E.x += cf;
+                        F.x += df;
+                        Cl = fmaf(xp, cf, Cl);
+                        Dl = fmaf(xp2.x, df, Dl);
+                        if (CROSS) Gc.x = fmaf(aGl, df, Gc.x);
                     }
-                    col_terms<MODEL, P>(gs, hs, xp, xd1, xd2, xs1, xs2, A[0] + A[1], B[0] + B[1],
-                                        E[0] + E[1], F[0] + F[1], Gc[0] + Gc[1], ax, aw);
+                    col_terms<MODEL, P>(gs, hs, xp, xd1, xd2, xs1, xs2, A.x + A.y, B.x + B.y,
+                                        E.x + E.y, F.x + F.y, Gc.x + Gc.y, ax, aw);
                     if (PIPE && j < BOX) {
                         tmem_ld_wait<LW>(nv);
 #pragma unroll
@@ -1770,9 +1829,13 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
                 columns(std::false_type{});
             }
 #pragma unroll
-            for (int t = 0; t < BOX; t++)
+            for (int t = 0; t < BOX; t++) {
+                const bool pr = t < 2 * NPR;
+                const float Ct = pr ? ((t & 1) ? CP[t >> 1].y : CP[t >> 1].x) : Cl;
+                const float Dt = pr ? ((t & 1) ? DP[t >> 1].y : DP[t >> 1].x) : Dl;
                 row_terms<MODEL, P>(gs, hs, yd1[t], yd2[t], SIG ? ys1[t] : 0.f,
-                                    SIG ? ys2[t] : 0.f, C[t], D[t], ay, aw);
+                                    SIG ? ys2[t] : 0.f, Ct, Dt, ay, aw);
+            }
             newton_step<P>(th, gs, hs, a);
         } else {
             float llr = 0.f;
@@ -1828,18 +1891,13 @@ __device__ __forceinline__ void fit_rois_r1(const KernelArgs &a, int64_t roi0, i
 // the first tile and frees it after the last; no path leaves the kernel
 // between the two.
 //
-// Residency: XYNBS 9x9 sCMOS asks for four blocks per SM (128 registers; its
-// shared memory would allow five and its tensor memory four), where its 163
-// registers gave three: 500 000 ROIs 1.060 -> 0.990 ms, the mixed batch
-// 343.6 -> 348.0 M fits/s (the table kernel spills 76 bytes and runs as
-// before).  Every other kernel passes 0, i.e. no minimum: an explicit 1 lets
-// the compiler take up to 255 registers (XYNB 11x11 sCMOS: 251 instead of
-// 142, two blocks per SM instead of three).
-template <int MODEL, int BOX, bool SCMOS>
-constexpr int r1_min_blocks() { return (MODEL == 1 && BOX == 9 && SCMOS) ? 4 : 0; }
-
+// Residency: no minimum of blocks per SM (an explicit 1 lets the compiler
+// take up to 255 registers: XYNB 11x11 sCMOS 251 instead of 142, two blocks
+// per SM instead of three).  XYNBS 9x9 sCMOS measured 0.962 ms for 500 000
+// ROIs when held to 128 registers for a fourth block (with 52 bytes of
+// spills), 0.952 ms with its own 164 registers and three blocks.
 template <int MODEL, int BOX, bool SCMOS, bool TABLE, bool LM = false>
-__global__ void __launch_bounds__(128, (LM ? 0 : r1_min_blocks<MODEL, BOX, SCMOS>()))
+__global__ void __launch_bounds__(128)
     fit_kernel_r1(const KernelArgs a, const TileTable t)
 {
     extern __shared__ __align__(16) float smem[];
