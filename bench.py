@@ -54,11 +54,11 @@ WORKLOAD = ("mixed-batch: 40% XYNB 11x11, 25% XYNBS 9x9, 15% XYNBSXSY 13x13, "
 # captured launch); the roofline's traffic scales it to the timed launch.
 TRAFFIC_BYTES_PER_ROI: dict[str, float] = {
     # 90 000 ROIs, one thread per ROI, 128 ROIs/block (variances in tensor
-    # memory, per-warp staging): 168.8 MB read + 4.8 MB written
-    "fit_kernel_r1<3, 15, true, false>": 1928.0,
+    # memory, per-warp staging, packed pixel loop): 155.5 MB read + 5.2 MB written
+    "fit_kernel_r1<3, 15, true, false>": 1785.3,
     # 240 000 ROIs, one thread per ROI, 128 ROIs/block (variances in tensor
-    # memory): 199.4 MB read + 8.9 MB written
-    "fit_kernel_r1<0, 11, true, false>": 867.9,
+    # memory, packed pixel loop): 195.7 MB read + 8.6 MB written
+    "fit_kernel_r1<0, 11, true, false>": 851.4,
 }
 
 
@@ -261,9 +261,9 @@ def measured_peaks() -> dict:
 
 def kernel_roofline(torch, dev, model, box, camera, n, seconds, sgemm_tinst=None) -> dict:
     """Roofline of one fit launch (gaussmle_gb300.roofline): the bound is the
-    slowest of issue (FP32 + SFU + FP64 lane instructions at 128 per SM per
-    clock), the SFU pipe, the FP64 pipe and HBM, each at its peak.  The issue
-    peak is taken at the GPU's maximum SM clock (MEASURED_PEAKS.json)."""
+    slowest of the FP32 pipe (FP32 lane operations at 128 per SM per clock),
+    the SFU pipe, the FP64 pipe and HBM, each at its peak.  The FP32 peak is
+    taken at the GPU's maximum SM clock (MEASURED_PEAKS.json)."""
     from gaussmle_gb300 import roofline
     peaks = measured_peaks()
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
@@ -272,10 +272,11 @@ def kernel_roofline(torch, dev, model, box, camera, n, seconds, sgemm_tinst=None
     r = roofline.roofline(model, box, camera, n, seconds, sms, mhz, hbm)
     out = {"bound": r["bound"], "achieved": r["achieved_tinst"], "peak": r["peak_tinst"],
            "unit": "Tinst/s", "frac": r["frac"], "pipe_frac": r["pipe_frac"],
+           "issue_unpacked_frac": r["issue_unpacked_frac"],
            "work_per_roi": r["work"], "bytes_per_roi": r["bytes_per_roi"],
            "hbm": {"achieved_gbs": n * r["bytes_per_roi"] / seconds / 1e9, "peak_gbs": hbm,
                    "frac": r["pipe_frac"]["hbm"]},
-           "peak_source": (f"issue peak {sms} SMs x 128 lanes x {mhz:.0f} MHz "
+           "peak_source": (f"FP32 peak {sms} SMs x 128 lanes x {mhz:.0f} MHz "
                            f"({'MEASURED_PEAKS.json' if 'source' not in peaks else 'fallback'}"
                            " sm_max_mhz); HBM: measured copy bandwidth")}
     if sgemm_tinst is not None:
@@ -724,7 +725,7 @@ def run_ours(args):
 
     if rank != 0:
         return
-    # ---- roofline of the dominant kernel: issue-bound FP32 + SFU + FP64 work ----
+    # ---- roofline of the dominant kernel: FP32, SFU and FP64 pipes and HBM ----
     # (the batch plan gives each group of >= 65536 ROIs its own plain launch)
     k = int(np.argmax(per_group))
     gk = groups[k]

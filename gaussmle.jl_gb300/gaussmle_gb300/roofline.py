@@ -3,18 +3,20 @@
 The fit has no dense contraction, so no tensor-core peak applies.  Its bound
 is the slowest of the resources one ROI uses, each at its peak:
   * HBM:  algorithmic bytes in and out / HBM bandwidth;
-  * issue: every FP32, SFU (MUFU) and FP64 lane instruction takes an issue
-    slot, and an SM issues at most 128 lane instructions per clock (4
-    schedulers x 32 lanes), which is also the FP32 pipe's rate;
-  * SFU:  16 MUFU lanes per SM per clock, i.e. a MUFU instruction holds its
-    pipe for 8 FP32 issue slots;
+  * FP32: the FMA pipes take 128 FP32 lane operations per SM per clock
+    (4 schedulers x 32 lanes).  A packed .f32x2 instruction issues two of
+    them in one slot but still takes two lanes of the pipe, so the FP32
+    operation count, not the instruction count, bounds the time;
+  * SFU:  16 MUFU lanes per SM per clock, i.e. a MUFU operation holds its
+    pipe for 8 FP32 slots;
   * FP64: about 2 lanes per SM per clock on GB300 (1/64 of FP32).
 The pipes run concurrently, so the instruction bound of a ROI is
-  max(fp32 + sfu + fp64,  8 sfu,  64 fp64)   FP32 lane-instruction slots
+  max(fp32,  8 sfu,  64 fp64)   FP32 lane slots
 (``work_per_roi()["slots"]``), and the roofline time of n ROIs is
-  max(n bytes / HBM, n slots / issue peak).
-``fp32_equiv_sum`` = fp32 + 8 sfu + 64 fp64 treats the pipes as if they never
-overlapped; it is kept only as a labelled pessimistic variant.
+  max(n bytes / HBM, n slots / FP32 peak).
+Two labelled variants are kept beside it: ``issue`` = fp32 + sfu + fp64, the
+issue slots the work takes when no FP32 operation is packed, and
+``fp32_equiv_sum`` = fp32 + 8 sfu + 64 fp64, as if the pipes never overlapped.
 
 Counts follow the minimum of the algorithm the kernel implements, which is
 already far below the reference's per-pixel recomputation
@@ -50,11 +52,12 @@ def _c(erf=0, exp=0, log=0, rcp=0, div=0, sqrt=0, fp32=0):
 
 
 def work_per_roi(model: int, box: int, iterations: int = 20, camera: int = 0) -> dict:
-    """Lane-instruction counts of one ROI fit (see the module docstring).
+    """Lane-operation counts of one ROI fit (see the module docstring).
 
-    Returns fp32, sfu, fp64 (lane instructions), issue (= their sum), slots
-    (the overlapping-pipe bound in FP32 lane slots, the roofline's work) and
-    fp32_equiv_sum (the non-overlapping variant)."""
+    Returns fp32, sfu, fp64 (lane operations), issue (= their sum: the issue
+    slots without packing), slots (the overlapping-pipe bound in FP32 lane
+    slots, the roofline's work) and fp32_equiv_sum (the non-overlapping
+    variant)."""
     P = NPARAMS[model]
     sig = model != 0
     scmos = camera != 0
@@ -93,7 +96,7 @@ def work_per_roi(model: int, box: int, iterations: int = 20, camera: int = 0) ->
     sfu = iterations * it[1] + fin[1]
     issue = fp32 + sfu + fp64
     return {"fp32": fp32, "sfu": sfu, "fp64": fp64, "issue": issue,
-            "slots": max(issue, SFU_SLOTS * sfu, FP64_SLOTS * fp64),
+            "slots": max(fp32, SFU_SLOTS * sfu, FP64_SLOTS * fp64),
             "fp32_equiv_sum": fp32 + SFU_SLOTS * sfu + FP64_SLOTS * fp64}
 
 
@@ -112,7 +115,8 @@ def bytes_per_roi(model: int, box: int, camera: int = 0, flags: bool = True) -> 
 
 
 def issue_peak_tinst(sm_count: int, sm_mhz: float) -> float:
-    """FP32 issue peak of the GPU [T lane instructions/s]: 128 per SM per clock."""
+    """FP32 peak of the GPU [T lane operations/s]: 128 per SM per clock (also
+    the issue rate of unpacked lane instructions)."""
     return sm_count * LANES_PER_SM * sm_mhz * 1e6 / 1e12
 
 
@@ -124,13 +128,14 @@ def roofline(model: int, box: int, camera: int, n: int, seconds: float, sm_count
     w = work_per_roi(model, box, iterations, camera)
     b = bytes_per_roi(model, box, camera)
     peak = issue_peak_tinst(sm_count, sm_mhz)             # T FP32 lane slots/s
-    t_issue = n * w["issue"] / (peak * 1e12)
+    t_fp32 = n * w["fp32"] / (peak * 1e12)
     t_sfu = n * w["sfu"] * SFU_SLOTS / (peak * 1e12)
     t_fp64 = n * w["fp64"] * FP64_SLOTS / (peak * 1e12)
     t_hbm = n * b / (hbm_gbs * 1e9)
-    terms = {"issue": t_issue, "sfu": t_sfu, "fp64": t_fp64, "hbm": t_hbm}
+    terms = {"fp32": t_fp32, "sfu": t_sfu, "fp64": t_fp64, "hbm": t_hbm}
     bound = max(terms, key=terms.get)
     return {"bound": bound, "frac": terms[bound] / seconds,
             "achieved_tinst": n * w["slots"] / seconds / 1e12, "peak_tinst": peak,
             "pipe_frac": {k: v / seconds for k, v in terms.items()},
+            "issue_unpacked_frac": n * w["issue"] / (peak * 1e12) / seconds,
             "work": w, "bytes_per_roi": b}

@@ -117,21 +117,20 @@ def test_roofline_model_counts():
     w11 = roofline.work_per_roi(0, 11, 20, 0)
     w13 = roofline.work_per_roi(1, 13, 20, 2)
     assert w11["slots"] < w13["slots"]
-    # the overlapping-pipe bound: the largest of issue, SFU and FP64 time
-    assert w11["slots"] == max(w11["issue"], 8 * w11["sfu"], 64 * w11["fp64"])
-    assert w11["fp32_equiv_sum"] > w11["slots"]
+    # the overlapping-pipe bound: the largest of FP32, SFU and FP64 time
+    assert w11["slots"] == max(w11["fp32"], 8 * w11["sfu"], 64 * w11["fp64"])
+    assert w11["issue"] == w11["fp32"] + w11["sfu"] + w11["fp64"] > w11["slots"]
+    assert w11["fp32_equiv_sum"] > w11["issue"]
     assert roofline.work_per_roi(0, 11, 10, 0)["fp32"] < w11["fp32"]
     assert roofline.bytes_per_roi(0, 11, 0) == 484 + 8 + 4 * 8 + 5
     assert roofline.bytes_per_roi(1, 13, 2) == 169 * 4 * 4 + 8 + 5 * 8 + 5
     # 1 ms for 10^6 ROIs: the fraction is the bound's time over the measured time
     r = roofline.roofline(0, 11, 2, 10 ** 6, 1e-3, 152, 2070.0, 6760.0)
-    assert r["bound"] == "issue"
-    assert abs(r["frac"] - 10 ** 6 * w11_scmos_issue() / 1e-3 / 40.27392e12) < 1e-9
+    assert r["bound"] == "fp32"
+    w = roofline.work_per_roi(0, 11, 20, 2)
+    assert abs(r["frac"] - 10 ** 6 * w["fp32"] / 1e-3 / 40.27392e12) < 1e-9
+    assert abs(r["issue_unpacked_frac"] - 10 ** 6 * w["issue"] / 1e-3 / 40.27392e12) < 1e-9
     assert abs(r["achieved_tinst"] / r["peak_tinst"] - r["frac"]) < 1e-12
-
-
-def w11_scmos_issue():
-    return roofline.work_per_roi(0, 11, 20, 2)["issue"]
 
 
 def test_library_without_gpu_fails_loudly():
