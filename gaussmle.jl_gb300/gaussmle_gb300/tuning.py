@@ -32,11 +32,18 @@ def load_cache(ctx: _lib.Context) -> int:
         return 0
     try:
         table = json.loads(CACHE.read_text()).get(_gpu_name(ctx.device), {})
-    except (OSError, ValueError):
+    except (OSError, ValueError, AttributeError):
+        return 0
+    if not isinstance(table, dict):
         return 0
     k = 0
-    for key, (tpr, rpb) in table.items():
-        m, b, cam = (int(v) for v in key.split("/"))
+    for key, shape in table.items():
+        try:
+            m, b, cam = (int(v) for v in key.split("/"))
+            tpr, rpb = (int(v) for v in shape)
+        except (TypeError, ValueError):
+            continue  # a malformed entry: keep the built-in default for that kind
+        # the library validates the shape and rejects one it cannot launch
         if ctx.lib.gmle_set_tuning(ctx.handle, m, b, cam, tpr, rpb) == 0:
             k += 1
     return k

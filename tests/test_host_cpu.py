@@ -1,5 +1,6 @@
 """CPU tests of the host-side mirror of the reference API (no GPU needed)."""
 import ctypes as C
+import json
 
 import numpy as np
 import pytest
@@ -140,3 +141,34 @@ def test_library_without_gpu_fails_loudly():
     with pytest.raises(G.GaussMLEError) as ei:
         G.Context(0)
     assert ei.value.status == 8  # GMLE_NO_DEVICE
+
+
+def test_tuning_cache_applies_this_gpus_entries_and_skips_malformed_ones(tmp_path, monkeypatch):
+    from gaussmle_gb300 import tuning
+    cache = tmp_path / "tuning.json"
+    monkeypatch.setattr(tuning, "CACHE", cache)
+    monkeypatch.setattr(tuning, "_gpu_name", lambda device: "GB300")
+
+    class FakeLib:
+        def __init__(self):
+            self.calls = []
+
+        def gmle_set_tuning(self, handle, m, b, cam, tpr, rpb):
+            self.calls.append((m, b, cam, tpr, rpb))
+            return 0 if tpr in (1, 2, 4, 8) else 1  # the library rejects a bad shape
+
+    class FakeCtx:
+        device, handle, lib = 0, None, FakeLib()
+
+    ctx = FakeCtx()
+    assert tuning.load_cache(ctx) == 0  # no cache file
+    cache.write_text(json.dumps({
+        "GB300": {"0/11/1": [1, 128], "3/15/0": [2, 64], "1/9/1": [3, 32],
+                  "bad key": [1, 32], "2/13/1": "x", "0/7/1": [1]},
+        "another GPU": {"0/11/0": [8, 16]}}))
+    assert tuning.load_cache(ctx) == 2
+    assert ctx.lib.calls == [(0, 11, 1, 1, 128), (3, 15, 0, 2, 64), (1, 9, 1, 3, 32)]
+    cache.write_text("[1, 2]")  # not a table
+    assert tuning.load_cache(ctx) == 0
+    cache.write_text("{")  # not JSON
+    assert tuning.load_cache(ctx) == 0
